@@ -1,0 +1,102 @@
+/*
+ * ufo_gb300.h -- C ABI of the GB300 tracking library (libufo_gb300.so).
+ *
+ * The reference (bellaz89/ufo) is pure Python: for every simulation object it
+ * generates an OpenCL C kernel with the lattice pasted in as literals, builds
+ * it with pyopencl and, in run(), copies the parameter pool to the device,
+ * launches the kernel and copies the result back.  This library replaces that
+ * generated kernel and its buffer plumbing with precompiled sm_103a kernels
+ * that interpret a lattice opcode table (built by ufo_gb300/compiler.py).
+ * Each entry point names the reference code it replaces.
+ *
+ * Conventions: every call returns 0 on success or a negative UFO_E* code;
+ * ufo_last_error() then returns a message (thread-local).  Host pointers are
+ * owned by the caller and only accessed during the call.  Calls on one
+ * context are not thread-safe (the reference's command queue was not either).
+ * Arithmetic is IEEE FP64.
+ */
+#ifndef UFO_GB300_H
+#define UFO_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define UFO_OK 0
+#define UFO_E_ARG (-1)       /* invalid argument (sizes, NULL, opcode table) */
+#define UFO_E_CUDA (-2)      /* CUDA runtime error */
+#define UFO_E_NOMEM (-3)     /* device allocation failed */
+#define UFO_E_TIMEOUT (-4)   /* a bounded device wait gave up */
+
+/* track modes: loss test at the end of each turn */
+#define UFO_MODE_TRACK 0     /* isnan(x)                        ufo/track.py:107-108 */
+#define UFO_MODE_SA 1        /* |x|>1 || |y|>1 || isnan(x)      ufo/sa.py:118-119    */
+
+/* track flags */
+#define UFO_TRACK_FMA 1      /* fused multiply-add arithmetic (tolerance parity) */
+#define UFO_TRACK_FIVED 2    /* do not write z, dp into tracks (ufo/track.py:62-65) */
+#define UFO_TRACK_PLAIN 4    /* one thread per particle, no lane refill */
+
+#define UFO_OP_WORDS 8
+
+typedef struct ufo_ctx ufo_ctx;    /* device, stream, scratch            */
+typedef struct ufo_prog ufo_prog;  /* a compiled line resident on device */
+
+/* Last error message of the calling thread ("" if none). */
+const char *ufo_last_error(void);
+
+/* Number of CUDA devices; replaces ufo/cl_utils.py:12-28 (list_devices). */
+int ufo_device_count(int *count);
+
+/* Create a context on `device` with its own stream; replaces the OpenCL
+ * context + command queue of ufo/cl_utils.py:30-33 and ufo/track.py:44-45. */
+int ufo_ctx_create(int device, ufo_ctx **out);
+void ufo_ctx_destroy(ufo_ctx *ctx);
+
+/* Upload a compiled line: `ops` int32[n_ops][8], `table` f64[n_seeds][stride],
+ * `n_dumps` observation points per turn.  Replaces the kernel build of
+ * ufo/track.py:84-118 (cl.Program(...).build). */
+int ufo_prog_create(ufo_ctx *ctx, const int32_t *ops, int n_ops, const double *table,
+                    int64_t stride, int n_seeds, int n_dumps, ufo_prog **out);
+/* Replace the per-seed constants (same stride); new parameter values between
+ * runs, the role of the reference's `.parameters` buffer for lattice values. */
+int ufo_prog_set_table(ufo_prog *prog, const double *table, int n_seeds);
+void ufo_prog_destroy(ufo_prog *prog);
+
+/*
+ * Track particles (host buffers, synchronous).  Replaces Track.run
+ * (ufo/track.py:125-139) + its kernel (:84-114) and StableAperture.run
+ * (ufo/sa.py:131-145) + its kernel (:93-126).
+ *   coords  f64[n][6]  x, px, y, py, z, dp at turn 0
+ *   seed    i32[n]     constant-table row of each particle, or NULL (row 0)
+ *   pturns  i32[n]     turns of each particle, or NULL (`turns` for all)
+ *   mode    UFO_MODE_TRACK / UFO_MODE_SA;  flags  UFO_TRACK_*
+ *   slots   observation slots per particle in `tracks` (count*turns/every);
+ *           0 disables tracks
+ *   every   observe on turns t with (t+1) % every == 0 (1 = every turn)
+ *   tracks  f64[n][slots][6] or NULL; unwritten slots are 0
+ *   lost    u32[n] or NULL: turn at whose end the particle was lost, else its
+ *           number of turns
+ *   final   f64[n][6] or NULL: coordinates after the last tracked turn
+ */
+int ufo_track(ufo_ctx *ctx, const ufo_prog *prog, const double *coords, const int32_t *seed,
+              const int32_t *pturns, int64_t n, int turns, int mode, int flags, int64_t slots,
+              int every, double *tracks, uint32_t *lost, double *final_state);
+
+/* Same, with device pointers, enqueued on `stream` (NULL: the context's
+ * stream) without synchronising; device buffers are the caller's. */
+int ufo_track_device(ufo_ctx *ctx, const ufo_prog *prog, const double *d_coords,
+                     const int32_t *d_seed, const int32_t *d_pturns, int64_t n, int turns,
+                     int mode, int flags, int64_t slots, int every, double *d_tracks,
+                     uint32_t *d_lost, double *d_final, void *stream);
+
+/* Kernel launches issued by this library since the context was created. */
+int ufo_launch_count(ufo_ctx *ctx, int64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,130 @@
+"""Shared test helpers: golden-fixture access and case runners."""
+import json
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(HERE)
+if REPO not in sys.path:
+    sys.path.insert(0, REPO)
+sys.path.insert(0, os.path.join(HERE, 'golden'))
+
+import latjson  # noqa: E402
+
+COORDS = ('x', 'px', 'y', 'py', 'z', 'dp')
+_gold = None
+
+
+def golden():
+    global _gold
+    if _gold is None:
+        with open(os.path.join(HERE, 'golden', 'cases.json')) as f:
+            meta = json.load(f)
+        arrs = dict(np.load(os.path.join(HERE, 'golden', 'golden.npz')))
+        _gold = (meta, arrs)
+    return _gold
+
+
+def cases(kind=None):
+    meta, _ = golden()
+    return [c for c in meta['cases'] if kind is None or c['kind'] == kind]
+
+
+def case(name):
+    for c in cases():
+        if c['name'] == name:
+            return c
+    raise KeyError(name)
+
+
+def arr(name, key):
+    return golden()[1][f'{name}/{key}']
+
+
+def line_of(c):
+    meta, _ = golden()
+    return latjson.load(meta['lattices'][c['lattice']])
+
+
+def coords_from_pool(pool, params, flags, dp=0.0):
+    n = pool.shape[0]
+    coords = np.zeros((n, 6))
+    for j, name in enumerate(COORDS):
+        if name in params:
+            coords[:, j] = pool[:, params.index(name)]
+    if flags & 2:  # FIVED
+        coords[:, 4] = 0.0
+        coords[:, 5] = dp
+    return coords
+
+
+def oracle_case(c):
+    """Run a golden track/sa case through the C oracle."""
+    from oracle import oracle as O
+    line = line_of(c)
+    params = latjson.params_load(c['parameters'])
+    pool = arr(c['name'], 'in/pool').astype(np.float64)
+    coords = coords_from_pool(pool, params, c['flags'], c.get('dp', 0.0))
+    n = pool.shape[0]
+    if c['kind'] == 'track':
+        return O.track(line, c['flags'], coords, c['turns'], parameters=params, where=c['where'],
+                       seed=np.arange(n), seed_values=pool, mode=0, dp=c.get('dp', 0.0))
+    return O.track(line, c['flags'], coords, c['turns'], parameters=params, where=[],
+                   seed=np.arange(n), seed_values=pool, mode=1, dp=c.get('dp', 0.0),
+                   tracks=False, count=0, dump_end=False)
+
+
+def gpu_case(c, extra_flags=0):
+    """Run a golden track/sa case through the public API on the GPU."""
+    import ufo_gb300 as u
+    line = line_of(c)
+    params = latjson.params_load(c['parameters'])
+    pool = arr(c['name'], 'in/pool')
+    flags = c['flags'] | extra_flags
+    if c['kind'] == 'track':
+        t = u.Track(line, flags=flags, turns=c['turns'], particles=pool.shape[0],
+                    parameters=params, where=c['where'], dp=c.get('dp', 0.0))
+        t.parameters[:] = pool
+        t.run()
+        return t
+    s = u.StableAperture(line, flags=flags, turns=c['turns'], particles=pool.shape[0],
+                         parameters=params, dp=c.get('dp', 0.0))
+    s.parameters[:] = pool
+    s.run()
+    return s
+
+
+def program_is_exact(prog):
+    """True when no op of the program evaluates a transcendental per particle
+    (those use the GPU's libm, which may differ from the host C library in
+    the last bit)."""
+    from ufo_gb300 import compiler as C
+    for row in prog.ops:
+        kind, flags = int(row[0]), int(row[1])
+        if kind in (C.OP_THICKQ, C.OP_THICKB) and not flags & C.F_CONST:
+            return False
+        if kind == C.OP_EDGE and flags & C.F_RTPSI:
+            return False
+        if kind == C.OP_WIRE:
+            return False
+    return True
+
+
+def track_rel_err(a, b):
+    """max |a-b| over written slots, relative to each coordinate's max |b|."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    scale = np.nanmax(np.abs(b).reshape(-1, b.shape[-1]), axis=0)
+    scale = np.where(scale > 0, scale, 1.0)
+    d = np.abs(a - b) / scale
+    both_nan = np.isnan(a) & np.isnan(b)
+    d = np.where(both_nan, 0.0, d)
+    return float(np.nanmax(np.where(np.isnan(d), np.inf, d))) if d.size else 0.0
+
+
+def tolerance(turns):
+    """FP64 agreement bar: 1e-12 relative after one turn, growing linearly to
+    1e-9 after 1000 turns."""
+    return 1e-12 * max(1, turns)

@@ -1,0 +1,134 @@
+"""Host-side logic: compiler folding and binding rules, aperture parsing,
+correctly rounded constant math, MAD-X loading, workloads."""
+import math
+
+import numpy as np
+import pytest
+
+import helpers as H
+import ufo_gb300 as u
+from ufo_gb300 import aperture as A
+from ufo_gb300 import compiler as C
+from ufo_gb300 import crmath, workloads as W
+
+
+def test_crmath_matches_mpmath():
+    mp = pytest.importorskip('mpmath')
+    mp.mp.prec = 200
+    rng = np.random.default_rng(1)
+    xs = list(rng.uniform(-3, 3, 300)) + [0.1034762088, 0.1963495408 / 1.3738850810, 1e-8, 2.5]
+    for x in xs:
+        for name in ('sin', 'cos', 'tan', 'sinh', 'cosh'):
+            want = float(getattr(mp, name)(mp.mpf(float(x))))
+            assert getattr(crmath, name)(x) == want, (name, x)
+
+
+def test_aperture_precedence_follows_c():
+    # 'a && b' pasted into `if (a && b == 0)` tests a && (b == 0)
+    code = A.compile_window('fabs(x) < 0.02 && fabs(y) < 0.005')
+    assert A.evaluate(code, x=0.01, y=0.01)          # a true, b false -> lost
+    assert not A.evaluate(code, x=0.01, y=0.001)     # a true, b true -> kept
+    assert not A.evaluate(code, x=0.05, y=0.01)      # a false -> kept
+    circle = A.compile_window('x*x + y*y < 1e-4')
+    assert A.evaluate(circle, x=0.02) and not A.evaluate(circle, x=0.005)
+    assert A.evaluate(A.compile_window(0))            # default window loses everything
+    assert A.evaluate(A.compile_window('1/2 > 0'))    # C integer division: 0 > 0 false -> lost
+    with pytest.raises(NotImplementedError):
+        A.compile_window('my_function(x) < 1')
+
+
+def test_teapot_constants_follow_reference_text():
+    # knl = ((k*L)*f)/N, outer = (L*f)/(2*(1+N)), inner = ((L*f - 2*outer)*px)/(N-1)
+    q = u.Quadrupole('q', length=0.3, k1=1.2, slices=4)
+    prog = C.compile_line(u.Line('l', [q]), u.KICK, where=[-1])
+    row = prog.ops[0]
+    assert row[0] == C.OP_TEAPOT
+    tab = prog.table[0]
+    L, f, N, k = 0.3, 1.0, 4, 1.2
+    outer = (L * f) / (2 * (1 + N))
+    assert tab[0] == outer
+    A_, d = (L * f - 2. * outer), N - 1.
+    assert tab[1] == A_ and tab[2] == d and tab[3] == 1.0 / d and tab[4] == A_ / d
+    assert tab[5] == ((0. + k) * L) * f / N
+
+
+def test_structural_zero_masks():
+    q = u.Quadrupole('q', length=0.3, k1=1.2, slices=4, dkn=[0., 0., 0.5])
+    prog = C.compile_line(u.Line('l', [q]), u.KICK, where=[-1])
+    slices, nn, ns, mn, ms = prog.ops[0][3:8]
+    assert (slices, nn, ns) == (4, 6, 0)   # pad([0,0,.5], 2) appends 3 zeros
+    assert mn == 0b110                     # k1 at index 1, dk2 at index 2
+
+
+def test_parameter_zero_in_one_seed_is_not_trimmed():
+    q = u.Quadrupole('q', length=0.3, k1=1.2, slices=4)
+    rows = np.array([[0.0], [0.3]])
+    prog = C.compile_line(u.Line('l', [q]), u.KICK, [('q', 'dk2')], [-1], seed_values=rows)
+    assert prog.ops[0][6] & 0b100
+    prog0 = C.compile_line(u.Line('l', [q]), u.KICK, [('q', 'dk2')], [-1],
+                           seed_values=rows[:1])
+    assert not prog0.ops[0][6] & 0b100
+
+
+def test_parameter_binding_quirks():
+    line = u.Line('l', [u.Drift('d', length=1.0), u.Quadrupole('q', length=0.3, k1=1.)])
+    # 'dp'[0] == 'd' binds to the element labelled 'd' (ufo/lattice.py:109)
+    with pytest.raises(TypeError):
+        C.compile_line(line, 0, ['dp'], [-1])
+    binds = C.element_bindings(line.flatten(), [('q', 'k1'), (1, 'dx'), ('q', 'k1')])
+    assert binds[1] == {'k1': 2, 'dx': 1}
+
+
+def test_fractures_follow_reference():
+    per, pre = C.fractures(4, [0, 0.5, 1.25, 2.75, -1])
+    assert pre == [True, False, False, False]
+    assert per[0] == [0.5] and per[1] == [0.25] and per[2] == [0.75] and per[3] == []
+
+
+def test_user_method_override_rejected():
+    class NLK(u.Multipole):
+        def method(self, **kw):
+            return ['x += 1;']
+    with pytest.raises(NotImplementedError):
+        C.compile_line(u.Line('l', [NLK('n', knl=[0, 1])]), 0, [], [-1])
+
+
+def test_madx_loader():
+    lat = u.Lattice()
+    from ufo_gb300 import madx
+    d = madx.loads('QF: QUADRUPOLE, L=0.3, K1= 1.2e0;\nO: DRIFT, L=1;\n'
+                   'B: SBEND, L=1.5, ANGLE=0.19, E1=0.1, HGAP=0.01, FINT=0.5;\n'
+                   'M: MULTIPOLE, KNL={0, 0, 3.5};\nX: FOO, A=1;\n'
+                   'C: LINE=(QF, O, B, M);\nR: LINE=(C, C);')
+    assert isinstance(d['R'], u.Line) and len(d['R'].flatten()) == 8
+    assert d['B'].hgap == 0.01 and d['M'].knl == [0, 0, 3.5]
+    with pytest.raises(TypeError):
+        madx.loads('Q: QUADRUPOLE, K9=1;')
+    assert lat is not None
+
+
+def test_golden_lattices_rebuild():
+    for c in H.cases():
+        line = H.line_of(c)
+        assert len(line.flatten()) > 0
+
+
+def test_workloads_shapes():
+    r1 = W.c1_ring(u)
+    assert len(r1.flatten()) == 128
+    r2 = W.c2_ring(u)
+    assert len(r2.flatten()) == 1024
+    M = W._linear_map(r2, 0.0)
+    assert abs((M[0, 0] + M[1, 1]) / 2) < 1 and abs((M[2, 2] + M[3, 3]) / 2) < 1
+    assert W.c3_grid().shape == (196608, 6)
+    parts, turns = W.c4_sizes()
+    assert parts.min() >= 256 and parts.max() <= 8192 and turns.min() >= 1000
+
+
+def test_flop_counts():
+    p1 = C.compile_line(W.c1_ring(u), u.KICK, where=[-1])
+    # teapot N=4: 2 outer drifts (4 each) + 3 inner drifts x*(px*A)/3 (6 each);
+    # quad kick 5, bend weak focusing 2 per slice; 4 plain drifts (4 each)
+    quad = 2 * 4 + 3 * 6 + 4 * 5
+    bend = 2 * 4 + 3 * 6 + 4 * 2
+    assert p1.flops == 16 * (2 * quad + 2 * bend + 4 * 4)

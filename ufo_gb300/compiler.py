@@ -1,0 +1,801 @@
+"""Lattice compiler: flattened line -> opcode table + per-seed FP64 constants.
+
+The reference turns a line into one straight-line OpenCL C function with every
+element constant pasted in as a literal (ufo/lattice.py:86-119 driving the
+templates of ufo/methods.py:16-241).  Here the same arithmetic is split into
+ * an opcode table shared by all particles of a launch (``Program.ops``,
+   int32 ``[n_ops, 8]``), which the sm_103a kernels interpret warp-uniformly,
+ * per-seed FP64 constant tables (``Program.table``, ``[n_seeds, stride]``),
+   one row per distinct setting of the lattice parameters.
+
+Bit-exactness rules (what makes the kernels reproduce the reference's FP64
+results to the last bit):
+ * Every constant sub-expression is folded here with IEEE double arithmetic in
+   the order the reference's C expression evaluates it (C is left-associative
+   and the templates paste text without parentheses, e.g. the inner teapot
+   drift is ``x += px * (A) / 3.0`` = ``(px*A)/3.0``, ufo/methods.py:81-82 and
+   :39-40).  Constants are folded per seed with numpy float64 arithmetic.
+ * Transcendentals of literal arguments are folded correctly rounded
+   (:mod:`ufo_gb300.crmath`), as GCC folds them; those of parameter-derived
+   values use the C library (``math``), as the reference calls it at run time.
+ * Terms whose coefficient is exactly zero in every seed ("structurally zero")
+   are dropped.  For finite coordinates the result is unchanged (up to the sign
+   of an exact zero); the kernels evaluate the full expression, zero terms
+   included, whenever x or y is not finite, so NaN/inf propagation is also the
+   reference's.
+
+Parameter binding mirrors ufo/lattice.py:107-110 (match on ``p[0]`` against
+the element label or its flat index, later entries overriding earlier ones)
+and the ``x or self.x`` resolution of the element ``method()``s.
+"""
+import math
+
+import numpy as np
+
+from . import aperture as _ap
+from . import crmath
+from . import elements as E
+from .flags import LINEAR, FIVED, EXACT, KICK, ACHROMATIC, YOSHIDA
+
+# ---- opcodes (shared with csrc/ufo_kernels.cuh and oracle) ----
+OP_NOP, OP_DRIFT, OP_KICK, OP_TEAPOT, OP_ALIGN, OP_EDGE, OP_THICKQ, OP_THICKB, OP_WIRE, \
+    OP_APERTURE, OP_OBSERVE = range(11)
+OP_NAMES = ['nop', 'drift', 'kick', 'teapot', 'align', 'edge', 'thickq', 'thickb', 'wire',
+            'aperture', 'observe']
+
+# drift forms: 0 -> x + px*c0 ; 1 -> x + (px*c0)*c1 ; 2 -> x + (px*c0)/c1
+DF_MUL, DF_MUL2, DF_DIV = 0, 1, 2
+
+# op flag bits
+F_ACHRO = 1 << 0        # no oodppo factor (ACHROMATIC)
+F_EXACT = 1 << 1        # exact drifts
+F_WEAK = 1 << 2         # teapot: weak-focusing term present
+F_RTPSI = 1 << 3        # edge: tan(psi) evaluated per particle
+F_T1 = 1 << 4           # edge: px term present
+F_T2 = 1 << 5           # edge: py term present
+F_CONST = 1 << 6        # thick: transcendentals folded per seed
+F_AX = 1 << 7           # align: x term present
+F_AY = 1 << 8           # align: y term present
+F_T1Z = 1 << 9          # edge: px term structurally zero (poison-only)
+F_T2Z = 1 << 10         # edge: py term structurally zero (poison-only)
+F_WEAKZ = 1 << 11       # teapot: weak term structurally zero (poison-only)
+F_YOSHIDA = 1 << 12     # teapot: 4th-order Yoshida splitting instead of TEAPOT
+# drift form of teapot outer/inner drifts packed in bits 16..19
+SH_FOUTER, SH_FINNER = 16, 18
+
+OP_WORDS = 8
+MAX_ORDERS = 32
+
+COORDS = ('x', 'px', 'y', 'py', 'z', 'dp')
+
+# Yoshida 4th-order coefficients (H. Yoshida, Phys. Lett. A 150 (1990) 262):
+# w1 = 1/(2 - 2^(1/3)), w0 = 1 - 2 w1; drift fractions c and kick fractions d.
+_Y_W1 = 1.0 / (2.0 - 2.0 ** (1.0 / 3.0))
+_Y_W0 = 1.0 - 2.0 * _Y_W1
+YOSHIDA_C = (_Y_W1 / 2.0, (_Y_W0 + _Y_W1) / 2.0, (_Y_W0 + _Y_W1) / 2.0, _Y_W1 / 2.0)
+YOSHIDA_D = (_Y_W1, _Y_W0, _Y_W1)
+
+
+class Val:
+    """A folded FP64 value over seeds: ``v`` is a numpy float64 array
+    ``[n_seeds]`` or a scalar; ``lit`` tells whether the reference would have
+    seen a literal (compile-time constant) rather than a parameter."""
+    __slots__ = ('v', 'lit')
+
+    def __init__(self, v, lit):
+        self.v = v
+        self.lit = lit
+
+    @staticmethod
+    def of(x, lit=True):
+        if isinstance(x, Val):
+            return x
+        return Val(np.float64(x) if np.ndim(x) == 0 else np.asarray(x, np.float64), lit)
+
+    def _bin(self, o, f):
+        o = Val.of(o)
+        with np.errstate(all='ignore'):
+            return Val(f(np.float64(self.v) if np.ndim(self.v) == 0 else self.v,
+                         np.float64(o.v) if np.ndim(o.v) == 0 else o.v), self.lit and o.lit)
+
+    def __add__(self, o): return self._bin(o, np.add)
+    def __sub__(self, o): return self._bin(o, np.subtract)
+    def __mul__(self, o): return self._bin(o, np.multiply)
+    def __truediv__(self, o): return self._bin(o, np.divide)
+    def __radd__(self, o): return Val.of(o)._bin(self, np.add)
+    def __rsub__(self, o): return Val.of(o)._bin(self, np.subtract)
+    def __rmul__(self, o): return Val.of(o)._bin(self, np.multiply)
+    def __rtruediv__(self, o): return Val.of(o)._bin(self, np.divide)
+
+    def __neg__(self):
+        return Val(-self.v, self.lit)
+
+    def zero(self):
+        """True when the value is +-0 in every seed (a structural zero)."""
+        return bool(np.all(np.asarray(self.v) == 0.0))
+
+    def finite_nonzero_everywhere(self):
+        a = np.asarray(self.v)
+        return bool(np.all(a != 0.0))
+
+
+def _fn(name, a):
+    """Math call on a folded value: correctly rounded for literals (GCC folds
+    them), the C library otherwise (the reference calls it at run time)."""
+    a = Val.of(a)
+    if name in ('sqrt', 'fabs'):
+        with np.errstate(all='ignore'):
+            return Val(np.sqrt(a.v) if name == 'sqrt' else np.abs(a.v), a.lit)
+    f = getattr(crmath, name) if a.lit else getattr(math, name)
+
+    def safe(x):
+        try:
+            return f(float(x))
+        except (ValueError, OverflowError):
+            return math.nan if name != 'cosh' else math.inf
+    if np.ndim(a.v) == 0:
+        return Val(np.float64(safe(a.v)), a.lit)
+    return Val(np.array([safe(x) for x in a.v]), a.lit)
+
+
+class Op:
+    """One opcode row plus its constants (each a Val)."""
+    __slots__ = ('kind', 'flags', 'ints', 'consts', 'elem', 'flops', 'flops_fast')
+
+    def __init__(self, kind, flags=0, ints=(), consts=(), elem=-1):
+        self.kind = kind
+        self.flags = flags
+        self.ints = list(ints)
+        self.consts = list(consts)
+        self.elem = elem
+        self.flops = 0
+        self.flops_fast = 0
+
+
+# ------------------------------------------------------------------ kicks
+
+def _pad(m, min_order):
+    """copy_multipoles_and_pad (ufo/methods.py:16-20): append max(len, min)
+    literal zeros."""
+    m = list(m)
+    m += [Val.of(0.0)] * max(len(m), min_order)
+    return m
+
+
+class KickSpec:
+    """Normal/skew coefficient lists of one kick, already scaled (teapot) and
+    truncated (LINEAR).  Coefficient j is structurally zero if zero in every
+    seed."""
+
+    def __init__(self, knl, ksl, flags):
+        self.achro = bool(flags & ACHROMATIC)
+        self.norm = self._trunc(knl, flags)
+        self.skew = self._trunc(ksl, flags)
+        for lst in (self.norm, self.skew):
+            if len(lst) > MAX_ORDERS:
+                raise NotImplementedError(f'more than {MAX_ORDERS} multipole orders')
+
+    @staticmethod
+    def _trunc(lst, flags):
+        # methods.kick: n = len(k); max_order = min(n, 2) if LINEAR else n
+        if not lst:
+            return []
+        n = len(lst)
+        mo = min(n, 2) if flags & LINEAR else n
+        return lst[:mo]
+
+    @staticmethod
+    def mask(lst):
+        m = 0
+        for j, c in enumerate(lst):
+            if not c.zero():
+                m |= 1 << j
+        return m
+
+    def packed(self):
+        """(n_norm, n_skew, mask_norm, mask_skew, consts) -- consts are the
+        structurally non-zero coefficients, normal then skew, ascending j."""
+        mn, ms = self.mask(self.norm), self.mask(self.skew)
+        consts = [c for j, c in enumerate(self.norm) if mn >> j & 1]
+        consts += [c for j, c in enumerate(self.skew) if ms >> j & 1]
+        return len(self.norm), len(self.skew), mn, ms, consts
+
+    def flops(self):
+        """Strict-mode FP64 operations of one kick (reference tree minus
+        structural zeros and exact identities), per kick."""
+        total = 0
+        for lst, skew in ((self.norm, False), (self.skew, True)):
+            total += _horner_flops(lst, self.achro, skew)
+        return total
+
+    def flops_fast(self):
+        total = 0
+        for lst, skew in ((self.norm, False), (self.skew, True)):
+            total += _horner_flops(lst, self.achro, skew, fast=True)
+        return total
+
+
+def _div_flops(order):
+    return 0 if order == 1 else 1
+
+
+def _horner_flops(lst, achro, skew, fast=False):
+    """Count the operations of methods.kick's Horner scheme (ufo/methods.py:
+    45-76) with structural zeros trimmed.  Fast mode counts an FMA as 2."""
+    n = len(lst)
+    if n == 0:
+        return 0
+    zx = lst[n - 1].zero()  # 'a' accumulator (dpx for normal, dpy for skew)
+    zy = True
+    f = 0
+    if not zx and not achro:
+        f += 1  # c * oodppo
+    for order in range(n - 1, 0, -1):
+        za = zx and zy
+        if not zx and not zy:
+            f += 3  # two products and one add/sub
+            f += 3  # second pair
+        elif not za:
+            f += 2  # one product each
+        if not za:
+            f += 2 * _div_flops(order)
+        zc = lst[order - 1].zero()
+        if not zc:
+            if not achro:
+                f += 1
+            if not za:
+                f += 1
+            zx = False
+        else:
+            zx = za
+        zy = za
+    if not zx:
+        f += 1
+    if not zy:
+        f += 1
+    return f
+
+
+# ------------------------------------------------------------------ lowering
+
+class _Lowerer:
+    def __init__(self, flags, n_seeds):
+        self.flags = flags
+        self.S = n_seeds
+        self.segments = [[]]   # list of lists of Op; dumps between segments
+
+    def emit(self, op):
+        self.segments[-1].append(op)
+
+    def new_segment(self):
+        self.segments.append([])
+
+    # -- primitive templates (ufo/methods.py) --
+    def align(self, dx, dy, elem):
+        """methods.align: x -= dx; y -= dy (ufo/methods.py:22-26).  A zero
+        offset is an exact identity (x - 0.0 == x, x - (-0.0) == x + 0)."""
+        dx, dy = Val.of(dx), Val.of(dy)
+        fl = (0 if dx.zero() else F_AX) | (0 if dy.zero() else F_AY)
+        if fl:
+            op = Op(OP_ALIGN, fl, consts=[dx, dy], elem=elem)
+            op.flops = op.flops_fast = bool(fl & F_AX) + bool(fl & F_AY)
+            self.emit(op)
+
+    def drift(self, form, c0, c1=None, elem=-1):
+        """methods.drift (ufo/methods.py:28-43) on the length text the caller
+        pasted: form DF_MUL ``L``, DF_MUL2 ``L * f``, DF_DIV ``(A) / d``."""
+        c0 = Val.of(c0)
+        if self.flags & EXACT:
+            # l = {length} / sqrt(...): the pasted length folds to one constant
+            if form == DF_MUL2:
+                lc = c0 * c1
+            elif form == DF_DIV:
+                lc = c0 / c1
+            else:
+                lc = c0
+            op = Op(OP_DRIFT, F_EXACT, ints=[DF_MUL], consts=[lc], elem=elem)
+            op.flops = op.flops_fast = 11
+            self.emit(op)
+            return
+        form, consts = self._drift_form(form, c0, c1)
+        op = Op(OP_DRIFT, 0, ints=[form], consts=consts, elem=elem)
+        op.flops = {DF_MUL: 4, DF_MUL2: 6, DF_DIV: 6}[form]
+        op.flops_fast = 4
+        self.emit(op)
+
+    @staticmethod
+    def _drift_form(form, c0, c1):
+        """Exact rewrites: (px*L)*1.0 == px*L; (px*A)/1.0 == px*A; (px*A)/2^k ==
+        px*(A/2^k) (scaling by a power of two commutes with rounding)."""
+        if form == DF_MUL2:
+            c1 = Val.of(c1)
+            if np.all(np.asarray(c1.v) == 1.0):
+                return DF_MUL, [c0]
+            return DF_MUL2, [c0, c1]
+        if form == DF_DIV:
+            c1 = Val.of(c1)
+            d = np.asarray(c1.v)
+            if np.all(d == d.flat[0]):
+                dv = float(d.flat[0])
+                m, e = math.frexp(dv)
+                if dv != 0 and m == 0.5 and math.isfinite(dv):
+                    return DF_MUL, [c0 / c1]
+            # (px*A)/d: the kernels divide by d exactly (Markstein correction with
+            # r = RN(1/d)); A/d serves the FMA mode's px*(A/d)
+            return DF_DIV, [c0, c1, 1.0 / c1, c0 / c1]
+        return DF_MUL, [c0]
+
+    def kick(self, knl, ksl, elem, weak=None):
+        ks = KickSpec(knl, ksl, self.flags)
+        nn, nsk, mn, ms, consts = ks.packed()
+        fl = F_ACHRO if self.flags & ACHROMATIC else 0
+        op = Op(OP_KICK, fl, ints=[nn, nsk, mn, ms], consts=consts, elem=elem)
+        op.flops = ks.flops()
+        op.flops_fast = ks.flops_fast()
+        self.emit(op)
+
+    def teapot(self, length, slices, knl, ksl, angle, elem, lenf):
+        """methods.teapot (ufo/methods.py:79-97).  ``length`` is the pasted
+        text ``L * f``: (L, f) with f the fracture fraction."""
+        L, f = length
+        Lf = Val.of(L) * f
+        if slices == 1:
+            outer = Lf / 2.0
+        else:
+            outer = Lf / float(2 * (1 + slices))
+        inner_a = Lf - 2.0 * outer
+        inner_d = Val.of(float(slices - 1.0))
+        # weak focusing: (A*f) * (A*f) * (L*f) / N / (L*f) / (L*f)
+        if angle is None:
+            weak = Val.of(0.0) * Lf / float(slices) / Lf / Lf
+        else:
+            A, fa = angle
+            Af = Val.of(A) * fa
+            weak = Af * Af * Lf / float(slices) / Lf / Lf
+        # coefficients: ({k}*{length}/{slices}) -> ((k*L)*f)/N
+        kn = [(Val.of(k) * L) * f / float(slices) for k in knl]
+        ksk = [(Val.of(k) * L) * f / float(slices) for k in ksl]
+        ks = KickSpec(kn, ksk, self.flags)
+        nn, nsk, mn, ms, kconsts = ks.packed()
+
+        fl = F_ACHRO if self.flags & ACHROMATIC else 0
+        if self.flags & YOSHIDA:
+            return self._yoshida(Lf, slices, ks, weak, elem)
+        exact = bool(self.flags & EXACT)
+        if exact:
+            fl |= F_EXACT
+            fo, oc = DF_MUL, [outer]
+            fi, ic = DF_MUL, [inner_a / inner_d]
+        else:
+            fo, oc = DF_MUL, [outer]
+            fi, ic = self._drift_form(DF_DIV, inner_a, inner_d)
+        if slices == 1:
+            fi, ic = DF_MUL, []
+        if not weak.zero():
+            fl |= F_WEAK
+            wc = [weak]
+        else:
+            fl |= F_WEAKZ
+            wc = []
+        fl |= fo << SH_FOUTER | fi << SH_FINNER
+        op = Op(OP_TEAPOT, fl, ints=[slices, nn, nsk, mn, ms], consts=oc + ic + kconsts + wc,
+                elem=elem)
+        dflops_o = 11 if exact else 4
+        dflops_i = 11 if exact else {DF_MUL: 4, DF_MUL2: 6, DF_DIV: 6}[fi]
+        wflops = 2 if fl & F_WEAK else 0
+        op.flops = 2 * dflops_o + (slices - 1) * dflops_i + slices * (ks.flops() + wflops)
+        fd = 11 if exact else 4
+        op.flops_fast = (slices + 1) * fd + slices * (ks.flops_fast() + wflops)
+        self.emit(op)
+
+    def _yoshida(self, Lf, slices, ks, weak, elem):
+        """Build's extra integrator: each of the N slices is a 4th-order
+        Yoshida drift-kick composition (3 kicks of weights d_i/N, 4 drifts of
+        c_i*L/N).  No reference counterpart."""
+        fl = F_YOSHIDA | (F_ACHRO if self.flags & ACHROMATIC else 0)
+        if self.flags & EXACT:
+            fl |= F_EXACT
+        n = len(ks.norm)
+        # kick coefficients scaled per slice are (k*L*f)/N; Yoshida weights
+        # multiply them, drifts are c_i * (L*f)/N
+        nn, nsk, mn, ms, kconsts = ks.packed()
+        dl = Lf / float(slices)
+        drifts = [dl * c for c in YOSHIDA_C]
+        wts = [Val.of(d) for d in YOSHIDA_D]
+        if not weak.zero():
+            fl |= F_WEAK
+            wc = [weak]
+        else:
+            fl |= F_WEAKZ
+            wc = []
+        op = Op(OP_TEAPOT, fl, ints=[slices, nn, nsk, mn, ms],
+                consts=drifts + wts + kconsts + wc, elem=elem)
+        op.flops = op.flops_fast = slices * (4 * 4 + 3 * (ks.flops() + 2 + (2 if wc else 0)))
+        self.emit(op)
+
+    def edge(self, length, angle, e, fringe, elem):
+        """methods.edge (ufo/methods.py:199-211) with the full (unfractured)
+        length and angle: curvature = angle/L (* oodppo);
+        psi = e - 2*curv*fringe/cos(e)*(1 + sin(e)*sin(e));
+        px += x*curv*tan(e); py -= y*curv*tan(psi)."""
+        achro = bool(self.flags & ACHROMATIC)
+        A = Val.of(angle) / Val.of(length)
+        e = Val.of(e)
+        fringe = Val.of(fringe)
+        cos_e = _fn('cos', e)
+        sin_e = _fn('sin', e)
+        onepss = 1.0 + sin_e * sin_e
+        t1 = _fn('tan', e)
+        fl = F_ACHRO if achro else 0
+        if achro:
+            psi = e - 2.0 * A * fringe / cos_e * onepss
+            t2 = _fn('tan', psi)
+            consts = [A, t1, t2]
+        elif fringe.zero():
+            # psi = e - (+-0) == e exactly for finite curvature
+            t2 = t1
+            consts = [A, t1, t2]
+        else:
+            fl |= F_RTPSI
+            consts = [A, t1, e, fringe, cos_e, onepss]
+        fl |= F_T1Z if t1.zero() else F_T1
+        if fl & F_RTPSI:
+            fl |= F_T2
+        else:
+            fl |= F_T2Z if consts[2].zero() else F_T2
+        op = Op(OP_EDGE, fl, consts=consts, elem=elem)
+        base = 0 if (achro or not fl & (F_T1 | F_T2)) else 1
+        op.flops = base + (3 if fl & F_T1 else 0) + (3 if fl & F_T2 else 0) + \
+            (7 if fl & F_RTPSI else 0)
+        op.flops_fast = op.flops
+        self.emit(op)
+
+    def thick_quad(self, L, f, k1, elem):
+        """methods.quadrupole thick branch (ufo/methods.py:99-134)."""
+        achro = bool(self.flags & ACHROMATIC)
+        k = Val.of(k1)
+        Lf = Val.of(L) * f
+        fl = F_ACHRO if achro else 0
+        consts = [k, Lf]
+        if achro:
+            k2 = _fn('sqrt', _fn('fabs', k))
+            k2l = Lf * k2
+            consts += [k2, _fn('cos', k2l), _fn('sin', k2l), _fn('cosh', k2l), _fn('sinh', k2l)]
+            fl |= F_CONST
+        op = Op(OP_THICKQ, fl, consts=consts, elem=elem)
+        op.flops = op.flops_fast = 16 + (0 if achro else 4)
+        self.emit(op)
+
+    def thick_bend(self, L, f, angle, k1, elem):
+        """methods.sbend thick branch (ufo/methods.py:136-196)."""
+        achro = bool(self.flags & ACHROMATIC)
+        Lf = Val.of(L) * f
+        Af = Val.of(angle) * f
+        c0 = Af / Lf
+        k1 = Val.of(k1)
+        fl = F_ACHRO if achro else 0
+        consts = [c0, k1, Lf]
+        if achro:
+            curv = c0
+            kv = k1
+            k2v = _fn('sqrt', _fn('fabs', kv))
+            k2lv = Lf * k2v
+            kx = kv + curv * curv
+            k2x = _fn('sqrt', _fn('fabs', kx))
+            k2lx = Lf * k2x
+            consts += [kv, k2v, _fn('cos', k2lv), _fn('sin', k2lv), _fn('cosh', k2lv),
+                       _fn('sinh', k2lv),
+                       kx, k2x, _fn('cos', k2lx), _fn('sin', k2lx), _fn('cosh', k2lx),
+                       _fn('sinh', k2lx), _fn('fabs', kx)]
+            fl |= F_CONST
+        op = Op(OP_THICKB, fl, consts=consts, elem=elem)
+        op.flops = op.flops_fast = 30 + (6 if not achro else 0)
+        self.emit(op)
+
+    def wire(self, x, y, k, elem):
+        op = Op(OP_WIRE, 0, consts=[Val.of(x), Val.of(y), Val.of(k)], elem=elem)
+        op.flops = op.flops_fast = 9
+        self.emit(op)
+
+    def aperture(self, window, elem):
+        code = _ap.compile_window(window)
+        consts = []
+        for opc, v in code:
+            consts += [Val.of(float(opc)), Val.of(float(v))]
+        op = Op(OP_APERTURE, 0, ints=[len(code)], consts=consts, elem=elem)
+        op.flops = op.flops_fast = sum(1 for opc, _ in code if opc in (
+            _ap.ADD, _ap.SUB, _ap.MUL, _ap.DIV, _ap.SQRT))
+        self.emit(op)
+
+
+def _mp_list(lst, name):
+    if isinstance(lst, str) or isinstance(lst, Val):
+        raise NotImplementedError(f'{name} cannot be a parameter as a whole vector; '
+                                  f'use the scalar names (e.g. dk2, k3s)')
+    return [Val.of(v) for v in lst]
+
+
+def _dk_from_kwargs(kwargs, dkn, dks):
+    """__dk_from_kwargs__ (ufo/elements.py:14-23): dkN / dkNs overrides,
+    padding the lists with zeros."""
+    for prm, value in kwargs.items():
+        if prm[:2] == 'dk' and prm[2:].isdigit():
+            idx = int(prm[2:])
+            dkn += [Val.of(0.0)] * (idx + 1 - len(dkn))
+            dkn[idx] = value
+        if prm[:2] == 'dk' and prm[-1:] == 's' and prm[2:-1].isdigit():
+            idx = int(prm[2:-1])
+            dks += [Val.of(0.0)] * (idx + 1 - len(dks))
+            dks[idx] = value
+
+
+def _resolve(elem, prm, name, default=None):
+    """``value = value or self.value``: a bound parameter always wins."""
+    if name in prm:
+        return prm[name]
+    return Val.of(getattr(elem, name, default) if default is None else
+                  getattr(elem, name, default))
+
+
+def lower_element(lw, elem, idx, prm, where):
+    """Lower one flat element.  ``prm`` maps attribute name -> Val (bound
+    parameters); ``where`` is its fracture list (fractions in [0, 1)).
+    Returns the number of code chunks emitted (segments = chunks - 1)."""
+    flags = lw.flags
+    if type(elem).method is not E.Element.method:
+        raise NotImplementedError(
+            f'{elem.label}: element overrides method(); user OpenCL pass methods cannot run '
+            f'in the data-driven GPU kernels')
+    kind = elem.kind
+    pieces = []
+    f0 = 0.0
+    for f in list(where) + [1.0]:
+        pieces.append(f - f0)
+        f0 = f
+
+    def chunks(emit_piece, prefix=None, suffix=None):
+        for i, fr in enumerate(pieces):
+            if i > 0:
+                lw.new_segment()
+            if i == 0 and prefix:
+                prefix()
+            emit_piece(fr)
+            if i == len(pieces) - 1 and suffix:
+                suffix()
+
+    if kind == 'marker':
+        return
+    if kind == 'drift':
+        # Drift.method takes no **kwargs (ufo/elements.py:98): other names raise
+        extra = [k for k in prm if k != 'length']
+        if extra:
+            raise TypeError(f"Drift.method() got an unexpected keyword argument '{extra[0]}'")
+        L = _resolve(elem, prm, 'length')
+        chunks(lambda fr: lw.drift(DF_MUL2, L, fr, elem=idx))
+        return
+    if kind == 'multipole':
+        knl = _mp_list(elem.knl, 'knl') if 'knl' not in prm else _mp_list(prm['knl'], 'knl')
+        ksl = _mp_list(elem.ksl, 'ksl') if 'ksl' not in prm else _mp_list(prm['ksl'], 'ksl')
+        dx = _resolve(elem, prm, 'dx')
+        dy = _resolve(elem, prm, 'dy')
+        for p, v in prm.items():
+            if p[:1] == 'k' and p[1:].isdigit():
+                knl[int(p[1:])] = v
+            if p[:1] == 'k' and p[-1:] == 's' and p[1:-1].isdigit():
+                ksl[int(p[1:-1])] = v
+        lw.align(dx, dy, idx)
+        lw.kick(knl, ksl, idx)
+        lw.align(-dx, -dy, idx)
+        return
+    if kind == 'wire':
+        lw.wire(_resolve(elem, prm, 'x'), _resolve(elem, prm, 'y'), _resolve(elem, prm, 'k'),
+                idx)
+        return
+    if kind == 'aperture':
+        lw.aperture(elem.window, idx)
+        return
+
+    slices = prm.get('slices', None)
+    if slices is not None:
+        raise NotImplementedError('slices cannot be a parameter')
+    slices = int(elem.slices)
+    L = _resolve(elem, prm, 'length')
+    dx = _resolve(elem, prm, 'dx')
+    dy = _resolve(elem, prm, 'dy')
+    dkn = _mp_list(elem.dkn, 'dkn') if 'dkn' not in prm else _mp_list(prm['dkn'], 'dkn')
+    dks = _mp_list(elem.dks, 'dks') if 'dks' not in prm else _mp_list(prm['dks'], 'dks')
+    _dk_from_kwargs(prm, dkn, dks)
+    align_in = lambda: lw.align(dx, dy, idx)
+    align_out = lambda: lw.align(-dx, -dy, idx)
+
+    if kind == 'quadrupole':
+        k1 = _resolve(elem, prm, 'k1')
+        if flags & KICK:
+            knl = _pad(dkn, 2)
+            knl[1] = knl[1] + k1
+            chunks(lambda fr: lw.teapot((L, fr), slices, knl, dks, None, idx, fr),
+                   align_in, align_out)
+        else:
+            chunks(lambda fr: lw.thick_quad(L, fr, k1, idx), align_in, align_out)
+        return
+    if kind in ('sbend', 'rbend'):
+        angle = _resolve(elem, prm, 'angle')
+        k1 = _resolve(elem, prm, 'k1')
+        e1 = _resolve(elem, prm, 'e1')
+        e2 = _resolve(elem, prm, 'e2')
+        hgap = _resolve(elem, prm, 'hgap')
+        fint = _resolve(elem, prm, 'fint')
+        fringe = Val.of(hgap) * Val.of(fint)
+        if kind == 'rbend':
+            e1 = e1 + angle * 0.5
+            e2 = e2 + angle * 0.5
+
+        def pre():
+            align_in()
+            lw.edge(L, angle, e1, fringe, idx)
+
+        def post():
+            lw.edge(L, angle, e2, fringe, idx)
+            align_out()
+        if flags & KICK:
+            knl = _pad(dkn, 2)
+            knl[1] = knl[1] + k1
+            chunks(lambda fr: lw.teapot((L, fr), slices, knl, dks, (angle, fr), idx, fr),
+                   pre, post)
+        else:
+            chunks(lambda fr: lw.thick_bend(L, fr, angle, k1, idx), pre, post)
+        return
+    if kind in ('sextupole', 'octupole'):
+        main = 'k2' if kind == 'sextupole' else 'k3'
+        order = 3 if kind == 'sextupole' else 4
+        kmain = _resolve(elem, prm, main)
+        knl = _pad(dkn, order)
+        knl[order - 1] = knl[order - 1] + kmain
+        # the reference passes dks, not the padded skew list (methods.py:219,227),
+        # so k2s / k3s never reach the kick
+        chunks(lambda fr: lw.teapot((L, fr), slices, knl, dks, None, idx, fr),
+               align_in, align_out)
+        return
+    raise NotImplementedError(f'element type {type(elem).__name__}')
+
+
+# ------------------------------------------------------------------ program
+
+class Program:
+    """A compiled line.
+
+    ops      int32 [n_ops, 8]   kind, flags, table offset, i0..i4
+    table    float64 [n_seeds, stride]
+    n_dumps  observation points executed per turn (D)
+    count    len(where) as the reference sizes its output (>= n_dumps)
+    """
+
+    def __init__(self, segments, n_seeds, n_elements, count, dump_end):
+        self.segments = segments
+        self.n_seeds = n_seeds
+        self.n_elements = n_elements
+        self.count = count
+        ops = []
+        consts = []
+        off = 0
+        dump = 0
+        self.flops = 0
+        self.flops_fast = 0
+        self.op_elem = []
+        for si, seg in enumerate(segments):
+            if si > 0:
+                ops.append([OP_OBSERVE, 0, 0, dump, 0, 0, 0, 0])
+                self.op_elem.append(-1)
+                dump += 1
+            for op in seg:
+                row = [op.kind, op.flags, off] + op.ints + [0] * (5 - len(op.ints))
+                ops.append(row)
+                self.op_elem.append(op.elem)
+                consts.extend(op.consts)
+                off += len(op.consts)
+                self.flops += op.flops
+                self.flops_fast += op.flops_fast
+        if dump_end:
+            ops.append([OP_OBSERVE, 0, 0, dump, 0, 0, 0, 0])
+            self.op_elem.append(-1)
+            dump += 1
+        self.n_dumps = dump
+        self.ops = np.ascontiguousarray(np.array(ops, dtype=np.int32).reshape(-1, OP_WORDS))
+        stride = max(off, 1)
+        table = np.zeros((n_seeds, stride), dtype=np.float64)
+        for j, c in enumerate(consts):
+            table[:, j] = c.v
+        self.table = np.ascontiguousarray(table)
+
+    @property
+    def n_ops(self):
+        return self.ops.shape[0]
+
+    def describe(self):
+        lines = []
+        for i, row in enumerate(self.ops):
+            lines.append(f'{i:5d} {OP_NAMES[row[0]]:8s} flags={row[1]:#x} toff={row[2]} '
+                         f'ints={list(row[3:])} elem={self.op_elem[i]}')
+        return '\n'.join(lines)
+
+
+def parse_parameters(parameters):
+    """Split the reference's parameter list into coordinate columns and lattice
+    bindings.  Returns (coord_cols {name: col}, bindings [(col, key, attr)])."""
+    coord_cols = {}
+    binds = []
+    for i, p in enumerate(parameters):
+        if isinstance(p, str) and p in COORDS:
+            coord_cols[p] = i
+        binds.append((i, p))
+    return coord_cols, binds
+
+
+def element_bindings(flat, parameters):
+    """For every flat element: {attr: column}, mirroring ufo/lattice.py:109-110
+    (``p[0] == label or p[0] == idx``; later columns override earlier)."""
+    out = []
+    for idx, elem in enumerate(flat):
+        prms = {}
+        for i, p in enumerate(parameters):
+            try:
+                key = p[0]
+            except (TypeError, IndexError):
+                continue
+            if key == elem.label or key == idx:
+                try:
+                    name = p[1]
+                except IndexError:
+                    raise IndexError(f'parameter {p!r} matches element {elem.label!r} '
+                                     f'but names no attribute')
+                prms[name] = i
+        out.append(prms)
+    return out
+
+
+def fractures(n, where):
+    """Per-element fracture lists and pre-element dump flags, mirroring
+    ufo/lattice.py:101-105."""
+    per = []
+    pre = []
+    for idx in range(n):
+        w = [f - idx for f in where if f != '*' and idx <= f < idx + 1]
+        if 0 in w:
+            w.remove(0)
+            pre.append(True)
+        else:
+            pre.append(False)
+        per.append(w)
+    return per, pre
+
+
+def compile_line(line, flags=0, parameters=(), where=(), seed_values=None, count=None,
+                 dump_end=None):
+    """Compile ``line`` for ``flags``.
+
+    seed_values : float64 [n_seeds, len(parameters)] -- the distinct rows of
+                  the parameter pool restricted to lattice columns (columns of
+                  coordinate parameters are ignored).  None -> one seed with
+                  every bound attribute = 0 (the value the reference's
+                  zero-initialised parameter buffer holds).
+    """
+    flat = line.flatten() if hasattr(line, 'flatten') else list(line)
+    parameters = list(parameters)
+    where = list(where)
+    if seed_values is None:
+        seed_values = np.zeros((1, max(len(parameters), 1)))
+    seed_values = np.asarray(seed_values, dtype=np.float64)
+    S = seed_values.shape[0]
+    lw = _Lowerer(flags, S)
+    binds = element_bindings(flat, parameters)
+    per, pre = fractures(len(flat), where)
+    for idx, elem in enumerate(flat):
+        if pre[idx]:
+            lw.new_segment()
+        prm = {name: Val(seed_values[:, col].copy(), False) for name, col in binds[idx].items()}
+        lower_element(lw, elem, idx, prm, per[idx])
+    if dump_end is None:
+        dump_end = -1 in where
+    if count is None:
+        count = len(where)
+    return Program(lw.segments, S, len(flat), count, dump_end)

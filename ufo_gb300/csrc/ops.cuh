@@ -1,0 +1,509 @@
+// ops.cuh -- FP64 element pass methods interpreted from the opcode table.
+//
+// Each op reproduces one template of the reference's code generator
+// (ufo/methods.py) with the reference's C evaluation order, so that in the
+// default (strict) mode every coordinate is bit-identical to the reference's
+// FP64 kernel.  Strict mode uses __dmul_rn/__dadd_rn/... (never contracted);
+// FMA mode contracts multiply-add pairs and replaces divisions by constants.
+//
+// Structurally-zero terms (coefficients that are 0 in every seed) were dropped
+// by the compiler.  For finite x, y the dropped terms contribute exact zeros;
+// when x or y is not finite, a 0*x term is NaN in the reference, so those
+// cases run the untrimmed expression (`slow` paths below).
+#pragma once
+#include <cstdint>
+
+namespace ufo {
+
+enum : int {
+  OP_NOP = 0, OP_DRIFT, OP_KICK, OP_TEAPOT, OP_ALIGN, OP_EDGE, OP_THICKQ, OP_THICKB, OP_WIRE,
+  OP_APERTURE, OP_OBSERVE
+};
+enum : int { DF_MUL = 0, DF_MUL2 = 1, DF_DIV = 2 };
+enum : int {
+  F_ACHRO = 1 << 0, F_EXACT = 1 << 1, F_WEAK = 1 << 2, F_RTPSI = 1 << 3, F_T1 = 1 << 4,
+  F_T2 = 1 << 5, F_CONST = 1 << 6, F_AX = 1 << 7, F_AY = 1 << 8, F_T1Z = 1 << 9,
+  F_T2Z = 1 << 10, F_WEAKZ = 1 << 11, F_YOSHIDA = 1 << 12
+};
+constexpr int SH_FOUTER = 16, SH_FINNER = 18;
+
+struct Op {
+  int kind, flags, toff, i0, i1, i2, i3, i4;
+};
+
+#define UFO_DEV __device__ __forceinline__
+
+UFO_DEV double mul(double a, double b) { return __dmul_rn(a, b); }
+UFO_DEV double add(double a, double b) { return __dadd_rn(a, b); }
+UFO_DEV double sub(double a, double b) { return __dsub_rn(a, b); }
+UFO_DEV double dvd(double a, double b) { return __ddiv_rn(a, b); }
+UFO_DEV double fma_(double a, double b, double c) { return __fma_rn(a, b, c); }
+UFO_DEV double ld(const double *p) { return __ldg(p); }
+
+// not finite: exponent field all ones (integer test, no FP64 pipe)
+UFO_DEV bool nf(double v) { return (__double2hiint(v) & 0x7ff00000) == 0x7ff00000; }
+
+// Correctly rounded a/d given r = RN(1/d): q0 = RN(a*r) is within an ulp of a/d
+// and Markstein's correction q = RN(q0 + RN(a - q0*d)*r) (the remainder is
+// exact under FMA) returns RN(a/d) (P. Markstein, IBM J. Res. Dev. 34 (1990);
+// Muller et al., Handbook of Floating-Point Arithmetic, ch. 4).  Operands far
+// from the unit range, zeros and non-finite values take IEEE division.
+UFO_DEV double divc(double a, double d, double r) {
+  const unsigned e = static_cast<unsigned>(__double2hiint(a)) & 0x7ff00000u;
+  if (e < 0x07700000u || e > 0x77f00000u) return dvd(a, d);
+  const double q0 = mul(a, r);
+  const double rem = fma_(-q0, d, a);
+  return fma_(rem, r, q0);
+}
+
+// reciprocals of the Horner orders 1..32, RN(1/k)
+__constant__ double c_rcp_order[33];
+
+UFO_DEV double div_order(double a, int order) {
+  if (order == 1) return a;
+  if (order == 2) return mul(a, 0.5);
+  if (order == 4) return mul(a, 0.25);
+  return divc(a, static_cast<double>(order), c_rcp_order[order]);
+}
+
+struct State {
+  double x, px, y, py, z, dp, o, opdp;  // o = 1/(1+dp); opdp = 1+dp (exact drift)
+  int turn;
+  bool bad_o;  // oodppo not finite: every kick takes the untrimmed path
+};
+
+// ---------------------------------------------------------------- drifts
+// methods.drift (ufo/methods.py:28-43) on the pasted length text
+template <bool FMA>
+UFO_DEV void drift(State &s, int form, bool exact, const double *c) {
+  if (exact) {
+    // l = {length} / sqrt(opdp*opdp - px*px - py*py): the length text folds to c[0]
+    const double l = dvd(ld(c), __dsqrt_rn(sub(sub(mul(s.opdp, s.opdp), mul(s.px, s.px)),
+                                                mul(s.py, s.py))));
+    if (FMA) {
+      s.x = fma_(s.px, l, s.x);
+      s.y = fma_(s.py, l, s.y);
+    } else {
+      s.x = add(s.x, mul(s.px, l));
+      s.y = add(s.y, mul(s.py, l));
+    }
+    return;
+  }
+  if (form == DF_MUL) {  // x += px * L
+    const double L = ld(c);
+    if (FMA) {
+      s.x = fma_(s.px, L, s.x);
+      s.y = fma_(s.py, L, s.y);
+    } else {
+      s.x = add(s.x, mul(s.px, L));
+      s.y = add(s.y, mul(s.py, L));
+    }
+  } else if (form == DF_MUL2) {  // x += px * L * f  ==  x + ((px*L)*f)
+    const double L = ld(c), f = ld(c + 1);
+    if (FMA) {
+      s.x = fma_(mul(s.px, L), f, s.x);
+      s.y = fma_(mul(s.py, L), f, s.y);
+    } else {
+      s.x = add(s.x, mul(mul(s.px, L), f));
+      s.y = add(s.y, mul(mul(s.py, L), f));
+    }
+  } else {  // x += px * (A) / d  ==  x + ((px*A)/d)
+    if (FMA) {
+      const double aod = ld(c + 3);
+      s.x = fma_(s.px, aod, s.x);
+      s.y = fma_(s.py, aod, s.y);
+    } else {
+      const double A = ld(c), d = ld(c + 1), r = ld(c + 2);
+      if (nf(s.px) || nf(s.py)) {
+        s.x = add(s.x, dvd(mul(s.px, A), d));
+        s.y = add(s.y, dvd(mul(s.py, A), d));
+      } else {
+        s.x = add(s.x, divc(mul(s.px, A), d, r));
+        s.y = add(s.y, divc(mul(s.py, A), d, r));
+      }
+    }
+  }
+}
+
+UFO_DEV int drift_nconst(int form, bool exact) {
+  return exact ? 1 : (form == DF_MUL ? 1 : form == DF_MUL2 ? 2 : 4);
+}
+
+// ---------------------------------------------------------------- kicks
+// methods.kick (ufo/methods.py:45-76).  Normal part, with a = dpx, b = dpy:
+//   a = c[n-1]*o; b = 0
+//   for order = n-1..1: na = (a*x - b*y)/order; nb = (a*y + b*x)/order;
+//                        a = c[order-1]*o + na; b = nb
+//   px -= a; py += b
+// Skew part, with a = dpy, b = dpx:
+//   na = (b*y + a*x)/order; nb = (b*x - a*y)/order; a = s[order-1]*o + na
+//   px -= b; py += a
+// `c` holds the structurally non-zero coefficients in ascending order.
+
+// untrimmed evaluation (reference semantics incl. 0*x terms) for non-finite x/y
+template <bool SKEW>
+UFO_DEV void horner_full(const State &s, int n, uint32_t mask, const double *c, bool achro,
+                         double &pxd, double &pyd) {
+  // coefficient j: its value if bit j is set, else a literal 0.
+  auto coef = [&](int j) -> double {
+    if (!((mask >> j) & 1u)) return 0.0;
+    return ld(c + __popc(mask & ((1u << j) - 1u)));
+  };
+  double a = achro ? coef(n - 1) : mul(coef(n - 1), s.o);
+  double b = 0.0;
+  for (int order = n - 1; order > 0; --order) {
+    double na, nb;
+    if (!SKEW) {
+      na = dvd(sub(mul(a, s.x), mul(b, s.y)), static_cast<double>(order));
+      nb = dvd(add(mul(a, s.y), mul(b, s.x)), static_cast<double>(order));
+    } else {
+      na = dvd(add(mul(b, s.y), mul(a, s.x)), static_cast<double>(order));
+      nb = dvd(sub(mul(b, s.x), mul(a, s.y)), static_cast<double>(order));
+    }
+    a = achro ? add(coef(order - 1), na) : add(mul(coef(order - 1), s.o), na);
+    b = nb;
+  }
+  if (!SKEW) {
+    pxd = a;
+    pyd = b;
+  } else {
+    pxd = b;
+    pyd = a;
+  }
+}
+
+// trimmed evaluation: za/zb mark exact (structural) zeros
+template <bool FMA, bool SKEW>
+UFO_DEV void horner_trim(const State &s, int n, uint32_t mask, const double *c, bool achro,
+                         double &pxd, bool &zpx, double &pyd, bool &zpy) {
+  int k = __popc(mask) - 1;  // index of the top non-zero coefficient in c
+  bool za = !((mask >> (n - 1)) & 1u), zb = true;
+  double a = 0.0, b = 0.0;
+  if (!za) {
+    a = achro ? ld(c + k) : mul(ld(c + k), s.o);
+    --k;
+  }
+  for (int order = n - 1; order > 0; --order) {
+    double na = 0.0, nb = 0.0;
+    const bool zn = za && zb;
+    if (!za && !zb) {
+      if (!SKEW) {
+        na = FMA ? fma_(a, s.x, -mul(b, s.y)) : sub(mul(a, s.x), mul(b, s.y));
+        nb = FMA ? fma_(a, s.y, mul(b, s.x)) : add(mul(a, s.y), mul(b, s.x));
+      } else {
+        na = FMA ? fma_(b, s.y, mul(a, s.x)) : add(mul(b, s.y), mul(a, s.x));
+        nb = FMA ? fma_(b, s.x, -mul(a, s.y)) : sub(mul(b, s.x), mul(a, s.y));
+      }
+    } else if (!za) {  // b is an exact zero
+      na = mul(a, s.x);
+      nb = SKEW ? -mul(a, s.y) : mul(a, s.y);
+    } else if (!zb) {  // a is an exact zero
+      na = SKEW ? mul(b, s.y) : -mul(b, s.y);
+      nb = mul(b, s.x);
+    }
+    if (!zn) {
+      na = div_order(na, order);
+      nb = div_order(nb, order);
+    }
+    if ((mask >> (order - 1)) & 1u) {
+      const double cc = ld(c + k);
+      --k;
+      if (achro)
+        a = zn ? cc : add(cc, na);
+      else
+        a = zn ? mul(cc, s.o) : (FMA ? fma_(cc, s.o, na) : add(mul(cc, s.o), na));
+      za = false;
+    } else {
+      a = na;
+      za = zn;
+    }
+    b = nb;
+    zb = zn;
+  }
+  if (!SKEW) {
+    pxd = a; zpx = za;
+    pyd = b; zpy = zb;
+  } else {
+    pxd = b; zpx = zb;
+    pyd = a; zpy = za;
+  }
+}
+
+// one kick; `bad` selects the untrimmed path.  nn/ns: list lengths, mn/ms: masks
+template <bool FMA>
+UFO_DEV void kick(State &s, int nn, int ns, uint32_t mn, uint32_t ms, const double *c,
+                  bool achro, bool bad) {
+  const double *cs = c + __popc(mn);
+  if (bad) {
+    if (nn) {
+      double a, b;
+      horner_full<false>(s, nn, mn, c, achro, a, b);
+      s.px = sub(s.px, a);
+      s.py = add(s.py, b);
+    }
+    if (ns) {
+      double a, b;
+      horner_full<true>(s, ns, ms, cs, achro, a, b);
+      s.px = sub(s.px, a);
+      s.py = add(s.py, b);
+    }
+    return;
+  }
+  if (nn) {
+    if (nn == 2 && mn == 2u) {
+      // quadrupole: px -= (K*o)*x; py += (K*o)*y
+      const double t = achro ? ld(c) : mul(ld(c), s.o);
+      if (FMA) {
+        s.px = fma_(-t, s.x, s.px);
+        s.py = fma_(t, s.y, s.py);
+      } else {
+        s.px = sub(s.px, mul(t, s.x));
+        s.py = add(s.py, mul(t, s.y));
+      }
+    } else if (nn == 3 && mn == 4u) {
+      // sextupole: a = ((K*o)*x)/2 = ((K*o)*0.5)*x exactly (power-of-two scaling)
+      const double t = mul(achro ? ld(c) : mul(ld(c), s.o), 0.5);
+      const double a = mul(t, s.x), b = mul(t, s.y);
+      if (FMA) {
+        s.px = fma_(b, s.y, fma_(-a, s.x, s.px));
+        s.py = fma_(b, s.x, fma_(a, s.y, s.py));
+      } else {
+        s.px = sub(s.px, sub(mul(a, s.x), mul(b, s.y)));
+        s.py = add(s.py, add(mul(a, s.y), mul(b, s.x)));
+      }
+    } else {
+      double a, b;
+      bool za, zb;
+      horner_trim<FMA, false>(s, nn, mn, c, achro, a, za, b, zb);
+      if (!za) s.px = sub(s.px, a);
+      if (!zb) s.py = add(s.py, b);
+    }
+  }
+  if (ns) {
+    double a, b;
+    bool za, zb;
+    horner_trim<FMA, true>(s, ns, ms, cs, achro, a, za, b, zb);
+    if (!za) s.px = sub(s.px, a);
+    if (!zb) s.py = add(s.py, b);
+  }
+}
+
+// weak focusing of a teapot slice: px -= x * W (ufo/methods.py:84)
+template <bool FMA>
+UFO_DEV void weak(State &s, int flags, double W, bool bad) {
+  if (flags & F_WEAK) {
+    s.px = FMA ? fma_(-s.x, W, s.px) : sub(s.px, mul(s.x, W));
+  } else if (bad) {
+    s.px = sub(s.px, mul(s.x, 0.0));  // structurally zero: only NaN/inf propagate
+  }
+}
+
+// ---------------------------------------------------------------- teapot
+// methods.teapot (ufo/methods.py:79-97): outer drift, N-1 x (kick, weak,
+// inner drift), kick, weak, outer drift.  Table: [outer][inner][kick][W].
+template <bool FMA>
+UFO_DEV void teapot(State &s, const Op &op, const double *c) {
+  const int N = op.i0, nn = op.i1, ns = op.i2;
+  const uint32_t mn = static_cast<uint32_t>(op.i3), ms = static_cast<uint32_t>(op.i4);
+  const bool exact = op.flags & F_EXACT, achro = op.flags & F_ACHRO;
+  const int fo = (op.flags >> SH_FOUTER) & 3, fi = (op.flags >> SH_FINNER) & 3;
+  const double *co = c;
+  const double *ci = co + drift_nconst(fo, exact);
+  const double *ck = ci + (N > 1 ? drift_nconst(fi, exact) : 0);
+  const double W = (op.flags & F_WEAK) ? ld(ck + __popc(mn) + __popc(ms)) : 0.0;
+  drift<FMA>(s, fo, exact, co);
+  for (int sl = 0; sl < N; ++sl) {
+    const bool bad = s.bad_o || nf(s.x) || nf(s.y);
+    kick<FMA>(s, nn, ns, mn, ms, ck, achro, bad);
+    weak<FMA>(s, op.flags, W, bad || nf(s.x));
+    if (sl < N - 1) drift<FMA>(s, fi, exact, ci);
+  }
+  drift<FMA>(s, fo, exact, co);
+}
+
+// ---------------------------------------------------------------- edge
+// methods.edge (ufo/methods.py:199-211):
+//   curvature = A (* o);  psi = e - 2*curv*fringe/cos(e)*(1 + sin(e)^2)
+//   px += x*curv*tan(e);  py -= y*curv*tan(psi)
+// table: [A, T1, T2] or, per-particle psi, [A, T1, e, fringe, cos e, 1+sin^2 e]
+UFO_DEV void edge(State &s, int flags, const double *c) {
+  const bool achro = flags & F_ACHRO;
+  // both terms structurally zero (e = psi = 0): only NaN/inf can propagate
+  if (!(flags & (F_T1 | F_T2)) && !(s.bad_o || nf(s.x) || nf(s.y))) return;
+  const double curv = achro ? ld(c) : mul(ld(c), s.o);
+  double t2;
+  if (flags & F_RTPSI) {
+    const double psi = sub(ld(c + 2), mul(dvd(mul(mul(2.0, curv), ld(c + 3)), ld(c + 4)),
+                                          ld(c + 5)));
+    t2 = tan(psi);
+  } else {
+    t2 = ld(c + 2);
+  }
+  const double x0 = s.x, y0 = s.y;
+  const bool bad = nf(x0) || nf(y0) || nf(curv);
+  if (flags & F_T1)
+    s.px = add(s.px, mul(mul(x0, curv), ld(c + 1)));
+  else if (bad)
+    s.px = add(s.px, mul(mul(x0, curv), 0.0));
+  if (flags & F_T2)
+    s.py = sub(s.py, mul(mul(y0, curv), t2));
+  else if (bad)
+    s.py = sub(s.py, mul(mul(y0, curv), 0.0));
+}
+
+// ---------------------------------------------------------------- thick
+struct Trig { double C, S, CH, SH; };
+
+UFO_DEV Trig trig(double k2l) {
+  Trig t;
+  sincos(k2l, &t.S, &t.C);
+  t.CH = cosh(k2l);
+  t.SH = sinh(k2l);
+  return t;
+}
+
+// methods.quadrupole thick branch (ufo/methods.py:103-134);
+// table [k, L*f, (k2, C, S, CH, SH)]
+UFO_DEV void thick_quad(State &s, int flags, const double *c) {
+  const double k = ld(c), Lf = ld(c + 1);
+  double k2;
+  Trig t;
+  if (flags & F_CONST) {
+    k2 = ld(c + 2);
+    t.C = ld(c + 3); t.S = ld(c + 4); t.CH = ld(c + 5); t.SH = ld(c + 6);
+  } else {
+    k2 = __dsqrt_rn(fabs((flags & F_ACHRO) ? k : mul(k, s.o)));
+    t = trig(mul(Lf, k2));
+  }
+  const double x0 = s.x, px0 = s.px, y0 = s.y, py0 = s.py;
+  if (k > 0.) {
+    s.x = add(mul(t.C, x0), dvd(mul(t.S, px0), k2));
+    s.px = add(mul(mul(-t.S, x0), k2), mul(t.C, px0));
+    s.y = add(mul(t.CH, y0), dvd(mul(t.SH, py0), k2));
+    s.py = add(mul(mul(t.SH, y0), k2), mul(t.CH, py0));
+  } else {
+    s.x = add(mul(t.CH, x0), dvd(mul(t.SH, px0), k2));
+    s.px = add(mul(mul(t.SH, x0), k2), mul(t.CH, px0));
+    s.y = add(mul(t.C, y0), dvd(mul(t.S, py0), k2));
+    s.py = add(mul(mul(-t.S, y0), k2), mul(t.C, py0));
+  }
+}
+
+// methods.sbend thick branch (ufo/methods.py:140-196); table
+// [A/L, k1, L*f, (kv, k2v, Cv, Sv, CHv, SHv, kx, k2x, Cx, Sx, CHx, SHx, |kx|)]
+UFO_DEV void thick_bend(State &s, int flags, const double *c) {
+  const bool achro = flags & F_ACHRO;
+  const double Lf = ld(c + 2);
+  const double curv = achro ? ld(c) : mul(ld(c), s.o);
+  double k, k2;
+  Trig t;
+  const double x0 = s.x, px0 = s.px, y0 = s.y, py0 = s.py;
+  if (flags & F_CONST) {
+    k = ld(c + 3); k2 = ld(c + 4);
+    t.C = ld(c + 5); t.S = ld(c + 6); t.CH = ld(c + 7); t.SH = ld(c + 8);
+  } else {
+    k = achro ? ld(c + 1) : mul(ld(c + 1), s.o);
+    k2 = __dsqrt_rn(fabs(k));
+    t = trig(mul(Lf, k2));
+  }
+  if (k > 0.) {
+    s.y = add(mul(t.CH, y0), dvd(mul(t.SH, py0), k2));
+    s.py = add(mul(mul(t.SH, y0), k2), mul(t.CH, py0));
+  }
+  if (k < 0.) {
+    s.y = add(mul(t.C, y0), dvd(mul(t.S, py0), k2));
+    s.py = add(mul(mul(-t.S, y0), k2), mul(t.C, py0));
+  }
+  if (k == 0.) s.y = add(s.y, mul(Lf, py0));
+  double ak;
+  if (flags & F_CONST) {
+    k = ld(c + 9); k2 = ld(c + 10);
+    t.C = ld(c + 11); t.S = ld(c + 12); t.CH = ld(c + 13); t.SH = ld(c + 14);
+    ak = ld(c + 15);
+  } else {
+    k = add(k, achro ? mul(curv, curv) : dvd(mul(curv, curv), s.o));
+    k2 = __dsqrt_rn(fabs(k));
+    t = trig(mul(Lf, k2));
+    ak = fabs(k);
+  }
+  if (k > 0.) {
+    s.x = add(mul(t.C, x0), dvd(mul(t.S, px0), k2));
+    s.x = add(s.x, dvd(mul(mul(s.dp, curv), sub(1., t.C)), ak));
+    s.px = add(mul(mul(-t.S, x0), k2), mul(t.C, px0));
+    s.px = add(s.px, dvd(mul(mul(s.dp, curv), t.S), k2));
+  }
+  if (k < 0.) {
+    s.x = add(mul(t.CH, x0), dvd(mul(t.SH, px0), k2));
+    s.x = add(s.x, dvd(mul(mul(s.dp, curv), sub(t.CH, 1.)), ak));
+    s.px = add(mul(mul(t.SH, x0), k2), mul(t.CH, px0));
+    s.px = add(s.px, dvd(mul(mul(s.dp, curv), t.SH), k2));
+  }
+  if (k == 0.) s.x = add(s.x, mul(Lf, px0));
+}
+
+// ---------------------------------------------------------------- wire
+// methods.wire (ufo/methods.py:230-241); table [xw, yw, k]
+UFO_DEV void wire(State &s, const double *c) {
+  const double wx = ld(c), wy = ld(c + 1), wk = ld(c + 2);
+  const double alpha = atan2(sub(wy, s.y), sub(wx, s.x));
+  const double B = dvd(wk, hypot(sub(wx, s.x), sub(wy, s.y)));
+  double sa, ca;
+  sincos(alpha, &sa, &ca);
+  s.px = add(s.px, mul(B, ca));
+  s.py = add(s.py, mul(B, sa));
+}
+
+// ---------------------------------------------------------------- aperture
+// stack program of ``{window} == 0`` (ufo_gb300/aperture.py); table holds
+// (opcode, value) pairs.  Returns true when the particle is lost.
+UFO_DEV bool aperture_lost(const State &s, const double *c, int n) {
+  double st[16];
+  int sp = 0;
+  for (int i = 0; i < n; ++i) {
+    const int op = static_cast<int>(ld(c + 2 * i));
+    const double v = ld(c + 2 * i + 1);
+    if (op == 1) { st[sp++] = v; continue; }
+    if (op == 2) {
+      const int k = static_cast<int>(v);
+      st[sp++] = k == 0 ? s.x : k == 1 ? s.px : k == 2 ? s.y : k == 3 ? s.py : k == 4 ? s.z
+               : k == 5 ? s.dp : k == 6 ? s.o : static_cast<double>(s.turn);
+      continue;
+    }
+    if (op == 3) { st[sp - 1] = -st[sp - 1]; continue; }
+    if (op == 4) { st[sp - 1] = st[sp - 1] == 0 ? 1. : 0.; continue; }
+    if (op == 19) { st[sp - 1] = fabs(st[sp - 1]); continue; }
+    if (op == 20) { st[sp - 1] = __dsqrt_rn(st[sp - 1]); continue; }
+    if (op == 21) {
+      const double b = st[--sp], a = st[--sp], cc = st[--sp];
+      st[sp++] = cc != 0 ? a : b;
+      continue;
+    }
+    const double b = st[--sp], a = st[--sp];
+    double r;
+    switch (op) {
+      case 5: r = add(a, b); break;
+      case 6: r = sub(a, b); break;
+      case 7: r = mul(a, b); break;
+      case 8: r = dvd(a, b); break;
+      case 9: r = b != 0 ? trunc(dvd(a, b)) : __longlong_as_double(0x7ff8000000000000ll); break;
+      case 10: r = b != 0 ? fmod(a, b) : __longlong_as_double(0x7ff8000000000000ll); break;
+      case 11: r = a < b; break;
+      case 12: r = a <= b; break;
+      case 13: r = a > b; break;
+      case 14: r = a >= b; break;
+      case 15: r = a == b; break;
+      case 16: r = a != b; break;
+      case 17: r = (a != 0) && (b != 0); break;
+      default: r = (a != 0) || (b != 0); break;
+    }
+    st[sp++] = r;
+  }
+  return sp > 0 && st[sp - 1] != 0;
+}
+
+UFO_DEV void align(State &s, int flags, const double *c) {
+  if (flags & F_AX) s.x = sub(s.x, ld(c));
+  if (flags & F_AY) s.y = sub(s.y, ld(c + 1));
+}
+
+}  // namespace ufo

@@ -1,0 +1,525 @@
+// ufo_gb300.cu -- tracking kernels and the C ABI (include/ufo_gb300.h).
+//
+// One thread tracks one particle with its state in registers; all lanes of a
+// warp walk the same opcode table, so element dispatch is warp-uniform.  The
+// per-seed FP64 constants are read through the read-only cache (each warp's
+// lanes usually share a seed, so loads broadcast).
+//
+// track_kernel is persistent: a grid of a few warps per SM pulls particles from
+// a device counter.  At each turn boundary the lanes whose particle finished
+// (lost, or its turn count reached) write their results and refill from the
+// counter with one warp-aggregated atomicAdd (ballot + popc + rank), so warps
+// stay full while survival is uneven -- the FP64 pipe charges a warp
+// instruction the same whether 1 or 32 lanes are active.  This is the
+// reference's atomic work queue (ufo/track.py:110-112, ufo/sa.py:122-124) at
+// lane granularity instead of work-item granularity.
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "../../include/ufo_gb300.h"
+#include "ops.cuh"
+
+namespace ufo {
+
+struct TrackArgs {
+  const Op *ops;
+  int n_ops;
+  const double *table;
+  int64_t stride;
+  int n_seeds;
+  int n_dumps;
+  const double *coords;
+  const int32_t *seed;
+  const int32_t *pturns;
+  int64_t n;
+  int turns;
+  int mode;
+  int flags;
+  int64_t slots;
+  int every;
+  double *tracks;
+  uint32_t *lost;
+  double *final_state;
+  unsigned long long *queue;  // particles handed out so far
+};
+
+UFO_DEV void load_particle(State &s, const TrackArgs &a, int64_t p) {
+  const double *c = a.coords + p * 6;
+  s.x = c[0];
+  s.px = c[1];
+  s.y = c[2];
+  s.py = c[3];
+  s.z = c[4];
+  s.dp = c[5];
+  s.o = dvd(1., add(s.dp, 1.));  // oodppo = 1. / (dp + 1.)  (ufo/track.py:103)
+  s.opdp = add(1., s.dp);        // opdp = 1. + dp            (ufo/methods.py:32)
+  s.turn = 0;
+  s.bad_o = nf(s.o);
+}
+
+UFO_DEV void store_final(const State &s, const TrackArgs &a, int64_t p) {
+  if (a.lost) a.lost[p] = static_cast<uint32_t>(s.turn);
+  if (a.final_state) {
+    double *f = a.final_state + p * 6;
+    f[0] = s.x; f[1] = s.px; f[2] = s.y; f[3] = s.py; f[4] = s.z; f[5] = s.dp;
+  }
+}
+
+UFO_DEV void observe(const State &s, const TrackArgs &a, int64_t p, int k) {
+  if (!a.tracks) return;
+  if ((s.turn + 1) % a.every) return;
+  const int64_t slot = static_cast<int64_t>((s.turn + 1) / a.every - 1) * a.n_dumps + k;
+  if (slot >= a.slots) return;
+  double *t = a.tracks + (p * a.slots + slot) * 6;
+  t[0] = s.x; t[1] = s.px; t[2] = s.y; t[3] = s.py;
+  if (!(a.flags & UFO_TRACK_FIVED)) { t[4] = s.z; t[5] = s.dp; }
+}
+
+// one pass through the line
+template <bool FMA>
+UFO_DEV void one_turn(State &s, const TrackArgs &a, const double *tab, int64_t p) {
+  for (int i = 0; i < a.n_ops; ++i) {
+    const int4 w0 = __ldg(reinterpret_cast<const int4 *>(a.ops + i));
+    const int4 w1 = __ldg(reinterpret_cast<const int4 *>(a.ops + i) + 1);
+    const Op op{w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
+    const double *c = tab + op.toff;
+    switch (op.kind) {
+      case OP_TEAPOT:
+        teapot<FMA>(s, op, c);
+        break;
+      case OP_DRIFT:
+        drift<FMA>(s, op.i0, op.flags & F_EXACT, c);
+        break;
+      case OP_KICK: {
+        const bool bad = s.bad_o || nf(s.x) || nf(s.y);
+        kick<FMA>(s, op.i0, op.i1, static_cast<uint32_t>(op.i2), static_cast<uint32_t>(op.i3), c,
+                  op.flags & F_ACHRO, bad);
+        break;
+      }
+      case OP_ALIGN:
+        align(s, op.flags, c);
+        break;
+      case OP_EDGE:
+        edge(s, op.flags, c);
+        break;
+      case OP_THICKQ:
+        thick_quad(s, op.flags, c);
+        break;
+      case OP_THICKB:
+        thick_bend(s, op.flags, c);
+        break;
+      case OP_WIRE:
+        wire(s, c);
+        break;
+      case OP_APERTURE:
+        if (aperture_lost(s, c, op.i0)) s.x = __longlong_as_double(0x7ff8000000000000ll);
+        break;
+      case OP_OBSERVE:
+        observe(s, a, p, op.i0);
+        break;
+      default:
+        break;
+    }
+  }
+}
+
+UFO_DEV bool is_lost(const State &s, int mode) {
+  if (mode == UFO_MODE_TRACK) return isnan(s.x);
+  return fabs(s.x) > 1. || fabs(s.y) > 1. || isnan(s.x);
+}
+
+template <bool FMA>
+__global__ void __launch_bounds__(128) track_kernel(TrackArgs a) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  int64_t p = -1;
+  bool exhausted = false;
+  State s{};
+  int target = 0;
+  const double *tab = a.table;
+  while (true) {
+    // lanes without a particle take the next ones from the queue
+    const unsigned need = __ballot_sync(FULL, p < 0 && !exhausted);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(a.queue, static_cast<unsigned long long>(__popc(need)));
+      base = __shfl_sync(FULL, base, leader);
+      if (p < 0 && !exhausted) {
+        const int64_t q = static_cast<int64_t>(base) + __popc(need & lt_mask);
+        if (q < a.n) {
+          p = q;
+          load_particle(s, a, p);
+          target = a.pturns ? a.pturns[p] : a.turns;
+          tab = a.table + (a.seed ? static_cast<int64_t>(a.seed[p]) : 0) * a.stride;
+          if (target <= 0) {  // nothing to track
+            store_final(s, a, p);
+            p = -1;
+          }
+        } else {
+          exhausted = true;
+        }
+      }
+      continue;  // re-check: a lane that got a zero-turn particle needs another
+    }
+    if (__all_sync(FULL, p < 0)) break;
+    if (p >= 0) {
+      one_turn<FMA>(s, a, tab, p);
+      const bool lost = is_lost(s, a.mode);
+      if (!lost) ++s.turn;
+      if (lost || s.turn >= target) {
+        store_final(s, a, p);
+        p = -1;
+      }
+    }
+  }
+}
+
+// plain variant: one thread per particle, no refill (the reference's
+// one-work-item-per-particle launch shape, used for comparisons)
+template <bool FMA>
+__global__ void __launch_bounds__(128) track_plain_kernel(TrackArgs a) {
+  const int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (p >= a.n) return;
+  State s{};
+  load_particle(s, a, p);
+  const int target = a.pturns ? a.pturns[p] : a.turns;
+  const double *tab = a.table + (a.seed ? static_cast<int64_t>(a.seed[p]) : 0) * a.stride;
+  while (s.turn < target) {
+    one_turn<FMA>(s, a, tab, p);
+    if (is_lost(s, a.mode)) break;
+    ++s.turn;
+  }
+  store_final(s, a, p);
+}
+
+}  // namespace ufo
+
+// ======================================================================= C ABI
+
+struct ufo_ctx {
+  int device;
+  int sm_count;
+  cudaStream_t stream;
+  unsigned long long *queue;
+  std::atomic<int64_t> launches;
+};
+
+struct ufo_prog {
+  ufo_ctx *ctx;
+  ufo::Op *ops;
+  int n_ops;
+  double *table;
+  int64_t stride;
+  int n_seeds;
+  int n_dumps;
+};
+
+namespace {
+thread_local char g_err[512] = "";
+
+int fail(int code, const char *fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof g_err, fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *what) {
+  return fail(UFO_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define UFO_CUDA(call)                                  \
+  do {                                                  \
+    cudaError_t e_ = (call);                            \
+    if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
+  } while (0)
+
+bool g_const_ready[64] = {};
+
+int ensure_constants(int device) {
+  if (device < 0 || device >= 64) return fail(UFO_E_ARG, "device %d out of range", device);
+  if (g_const_ready[device]) return UFO_OK;
+  double r[33];
+  r[0] = 0.0;
+  for (int k = 1; k <= 32; ++k) r[k] = 1.0 / static_cast<double>(k);
+  UFO_CUDA(cudaMemcpyToSymbol(ufo::c_rcp_order, r, sizeof r));
+  g_const_ready[device] = true;
+  return UFO_OK;
+}
+
+int validate_ops(const int32_t *ops, int n_ops, int64_t stride) {
+  for (int i = 0; i < n_ops; ++i) {
+    const int32_t *w = ops + i * UFO_OP_WORDS;
+    if (w[0] < ufo::OP_NOP || w[0] > ufo::OP_OBSERVE)
+      return fail(UFO_E_ARG, "op %d: unknown kind %d", i, w[0]);
+    if (w[2] < 0 || (w[0] != ufo::OP_OBSERVE && w[0] != ufo::OP_NOP && w[2] >= stride))
+      return fail(UFO_E_ARG, "op %d: table offset %d outside stride %lld", i, w[2],
+                  static_cast<long long>(stride));
+    if (w[0] == ufo::OP_TEAPOT && (w[3] < 1 || w[4] < 0 || w[4] > 32 || w[5] < 0 || w[5] > 32))
+      return fail(UFO_E_ARG, "op %d: bad teapot shape", i);
+    if (w[0] == ufo::OP_KICK && (w[3] < 0 || w[3] > 32 || w[4] < 0 || w[4] > 32))
+      return fail(UFO_E_ARG, "op %d: bad kick shape", i);
+    if (w[0] == ufo::OP_APERTURE && (w[3] < 0 || w[2] + 2 * static_cast<int64_t>(w[3]) > stride))
+      return fail(UFO_E_ARG, "op %d: aperture program outside table", i);
+  }
+  return UFO_OK;
+}
+
+int launch_track(ufo_ctx *ctx, const ufo_prog *prog, const double *d_coords, const int32_t *d_seed,
+                 const int32_t *d_pturns, int64_t n, int turns, int mode, int flags, int64_t slots,
+                 int every, double *d_tracks, uint32_t *d_lost, double *d_final,
+                 cudaStream_t stream) {
+  if (n <= 0) return UFO_OK;
+  ufo::TrackArgs a;
+  a.ops = prog->ops;
+  a.n_ops = prog->n_ops;
+  a.table = prog->table;
+  a.stride = prog->stride;
+  a.n_seeds = prog->n_seeds;
+  a.n_dumps = prog->n_dumps;
+  a.coords = d_coords;
+  a.seed = d_seed;
+  a.pturns = d_pturns;
+  a.n = n;
+  a.turns = turns;
+  a.mode = mode;
+  a.flags = flags;
+  a.slots = d_tracks ? slots : 0;
+  a.every = every < 1 ? 1 : every;
+  a.tracks = d_tracks;
+  a.lost = d_lost;
+  a.final_state = d_final;
+  a.queue = ctx->queue;
+  const bool fma = flags & UFO_TRACK_FMA;
+  if (flags & UFO_TRACK_PLAIN) {
+    const int64_t blocks = (n + 127) / 128;
+    if (fma)
+      ufo::track_plain_kernel<true><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(a);
+    else
+      ufo::track_plain_kernel<false><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(a);
+  } else {
+    UFO_CUDA(cudaMemsetAsync(ctx->queue, 0, sizeof(unsigned long long), stream));
+    int64_t warps = (n + 31) / 32;
+    const int64_t max_warps = static_cast<int64_t>(ctx->sm_count) * 16;
+    if (warps > max_warps) warps = max_warps;
+    const int64_t blocks = (warps + 3) / 4;
+    if (fma)
+      ufo::track_kernel<true><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(a);
+    else
+      ufo::track_kernel<false><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(a);
+  }
+  ctx->launches.fetch_add(1);
+  UFO_CUDA(cudaGetLastError());
+  return UFO_OK;
+}
+
+int check_track_args(ufo_ctx *ctx, const ufo_prog *prog, int64_t n, int turns, int mode,
+                     int64_t slots, int every) {
+  if (!ctx || !prog) return fail(UFO_E_ARG, "null context or program");
+  if (prog->ctx != ctx) return fail(UFO_E_ARG, "program belongs to another context");
+  if (n < 0) return fail(UFO_E_ARG, "negative particle count");
+  if (turns < 0) return fail(UFO_E_ARG, "negative turn count");
+  if (mode != UFO_MODE_TRACK && mode != UFO_MODE_SA) return fail(UFO_E_ARG, "bad mode %d", mode);
+  if (slots < 0) return fail(UFO_E_ARG, "negative slot count");
+  if (every < 1) return fail(UFO_E_ARG, "every must be >= 1");
+  return UFO_OK;
+}
+}  // namespace
+
+extern "C" {
+
+const char *ufo_last_error(void) { return g_err; }
+
+int ufo_device_count(int *count) {
+  if (!count) return fail(UFO_E_ARG, "null count");
+  UFO_CUDA(cudaGetDeviceCount(count));
+  return UFO_OK;
+}
+
+int ufo_ctx_create(int device, ufo_ctx **out) {
+  if (!out) return fail(UFO_E_ARG, "null output");
+  *out = nullptr;
+  int n = 0;
+  UFO_CUDA(cudaGetDeviceCount(&n));
+  if (device < 0 || device >= n) return fail(UFO_E_ARG, "device %d of %d", device, n);
+  UFO_CUDA(cudaSetDevice(device));
+  int rc = ensure_constants(device);
+  if (rc) return rc;
+  ufo_ctx *c = new (std::nothrow) ufo_ctx;
+  if (!c) return fail(UFO_E_NOMEM, "host allocation");
+  c->device = device;
+  c->launches = 0;
+  cudaDeviceProp prop;
+  cudaError_t e = cudaGetDeviceProperties(&prop, device);
+  if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaGetDeviceProperties"); }
+  c->sm_count = prop.multiProcessorCount;
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaStreamCreate"); }
+  e = cudaMalloc(&c->queue, 64);
+  if (e != cudaSuccess) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return fail(UFO_E_NOMEM, "cudaMalloc(queue): %s", cudaGetErrorString(e));
+  }
+  *out = c;
+  return UFO_OK;
+}
+
+void ufo_ctx_destroy(ufo_ctx *ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(ctx->queue);
+  cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+int ufo_launch_count(ufo_ctx *ctx, int64_t *count) {
+  if (!ctx || !count) return fail(UFO_E_ARG, "null argument");
+  *count = ctx->launches.load();
+  return UFO_OK;
+}
+
+int ufo_prog_create(ufo_ctx *ctx, const int32_t *ops, int n_ops, const double *table,
+                    int64_t stride, int n_seeds, int n_dumps, ufo_prog **out) {
+  if (!ctx || !ops || !table || !out) return fail(UFO_E_ARG, "null argument");
+  *out = nullptr;
+  if (n_ops < 0 || stride < 1 || n_seeds < 1 || n_dumps < 0)
+    return fail(UFO_E_ARG, "bad program sizes");
+  int rc = validate_ops(ops, n_ops, stride);
+  if (rc) return rc;
+  UFO_CUDA(cudaSetDevice(ctx->device));
+  ufo_prog *p = new (std::nothrow) ufo_prog;
+  if (!p) return fail(UFO_E_NOMEM, "host allocation");
+  p->ctx = ctx;
+  p->n_ops = n_ops;
+  p->stride = stride;
+  p->n_seeds = n_seeds;
+  p->n_dumps = n_dumps;
+  p->ops = nullptr;
+  p->table = nullptr;
+  const size_t ob = sizeof(ufo::Op) * (n_ops > 0 ? n_ops : 1);
+  const size_t tb = sizeof(double) * static_cast<size_t>(stride) * n_seeds;
+  if (cudaMalloc(&p->ops, ob) != cudaSuccess || cudaMalloc(&p->table, tb) != cudaSuccess) {
+    cudaFree(p->ops);
+    cudaFree(p->table);
+    delete p;
+    return fail(UFO_E_NOMEM, "cudaMalloc(program %zu + %zu bytes)", ob, tb);
+  }
+  cudaError_t e = cudaMemcpyAsync(p->ops, ops, sizeof(ufo::Op) * n_ops, cudaMemcpyHostToDevice,
+                                  ctx->stream);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(p->table, table, tb, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    cudaFree(p->ops);
+    cudaFree(p->table);
+    delete p;
+    return cuda_fail(e, "program upload");
+  }
+  *out = p;
+  return UFO_OK;
+}
+
+int ufo_prog_set_table(ufo_prog *prog, const double *table, int n_seeds) {
+  if (!prog || !table) return fail(UFO_E_ARG, "null argument");
+  if (n_seeds != prog->n_seeds) return fail(UFO_E_ARG, "seed count changed");
+  UFO_CUDA(cudaSetDevice(prog->ctx->device));
+  const size_t tb = sizeof(double) * static_cast<size_t>(prog->stride) * n_seeds;
+  UFO_CUDA(cudaMemcpyAsync(prog->table, table, tb, cudaMemcpyHostToDevice, prog->ctx->stream));
+  UFO_CUDA(cudaStreamSynchronize(prog->ctx->stream));
+  return UFO_OK;
+}
+
+void ufo_prog_destroy(ufo_prog *prog) {
+  if (!prog) return;
+  cudaSetDevice(prog->ctx->device);
+  cudaStreamSynchronize(prog->ctx->stream);
+  cudaFree(prog->ops);
+  cudaFree(prog->table);
+  delete prog;
+}
+
+int ufo_track_device(ufo_ctx *ctx, const ufo_prog *prog, const double *d_coords,
+                     const int32_t *d_seed, const int32_t *d_pturns, int64_t n, int turns,
+                     int mode, int flags, int64_t slots, int every, double *d_tracks,
+                     uint32_t *d_lost, double *d_final, void *stream) {
+  int rc = check_track_args(ctx, prog, n, turns, mode, slots, every);
+  if (rc) return rc;
+  if (n > 0 && !d_coords) return fail(UFO_E_ARG, "null coordinates");
+  UFO_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+  return launch_track(ctx, prog, d_coords, d_seed, d_pturns, n, turns, mode, flags, slots, every,
+                      d_tracks, d_lost, d_final, st);
+}
+
+int ufo_track(ufo_ctx *ctx, const ufo_prog *prog, const double *coords, const int32_t *seed,
+              const int32_t *pturns, int64_t n, int turns, int mode, int flags, int64_t slots,
+              int every, double *tracks, uint32_t *lost, double *final_state) {
+  int rc = check_track_args(ctx, prog, n, turns, mode, slots, every);
+  if (rc) return rc;
+  if (n == 0) return UFO_OK;
+  if (!coords) return fail(UFO_E_ARG, "null coordinates");
+  if (seed) {
+    for (int64_t i = 0; i < n; ++i)
+      if (seed[i] < 0 || seed[i] >= prog->n_seeds)
+        return fail(UFO_E_ARG, "particle %lld: seed %d outside [0, %d)",
+                    static_cast<long long>(i), seed[i], prog->n_seeds);
+  }
+  UFO_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  const size_t cb = sizeof(double) * 6 * n;
+  const size_t tb = tracks ? sizeof(double) * 6 * static_cast<size_t>(slots) * n : 0;
+  double *d_coords = nullptr, *d_tracks = nullptr, *d_final = nullptr;
+  int32_t *d_seed = nullptr, *d_pturns = nullptr;
+  uint32_t *d_lost = nullptr;
+  auto cleanup = [&]() {
+    cudaFree(d_coords); cudaFree(d_tracks); cudaFree(d_final);
+    cudaFree(d_seed); cudaFree(d_pturns); cudaFree(d_lost);
+  };
+  if (cudaMalloc(&d_coords, cb) != cudaSuccess ||
+      (tb && cudaMalloc(&d_tracks, tb) != cudaSuccess) ||
+      (final_state && cudaMalloc(&d_final, cb) != cudaSuccess) ||
+      (seed && cudaMalloc(&d_seed, sizeof(int32_t) * n) != cudaSuccess) ||
+      (pturns && cudaMalloc(&d_pturns, sizeof(int32_t) * n) != cudaSuccess) ||
+      (lost && cudaMalloc(&d_lost, sizeof(uint32_t) * n) != cudaSuccess)) {
+    cleanup();
+    return fail(UFO_E_NOMEM, "device buffers for %lld particles", static_cast<long long>(n));
+  }
+  cudaError_t e = cudaMemcpyAsync(d_coords, coords, cb, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && seed)
+    e = cudaMemcpyAsync(d_seed, seed, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && pturns)
+    e = cudaMemcpyAsync(d_pturns, pturns, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && tb) e = cudaMemsetAsync(d_tracks, 0, tb, st);
+  if (e != cudaSuccess) {
+    cleanup();
+    return cuda_fail(e, "upload");
+  }
+  rc = launch_track(ctx, prog, d_coords, d_seed, d_pturns, n, turns, mode, flags, slots, every,
+                    d_tracks, d_lost, d_final, st);
+  if (rc) {
+    cleanup();
+    return rc;
+  }
+  e = cudaSuccess;
+  if (tb) e = cudaMemcpyAsync(tracks, d_tracks, tb, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && lost)
+    e = cudaMemcpyAsync(lost, d_lost, sizeof(uint32_t) * n, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess && final_state)
+    e = cudaMemcpyAsync(final_state, d_final, cb, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cleanup();
+  if (e != cudaSuccess) return cuda_fail(e, "track");
+  return UFO_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,418 @@
+"""Simulation drivers with the reference's class API, running on the GPU.
+
+``Track``, ``StableAperture``, ``ClosedOrbit`` and ``Optics`` keep the
+reference's constructor signatures, attributes (``parameters``, ``tracks``,
+``lost``, ``orbits``, ``track``, ``bx``...), ``run(threads)`` and error
+behaviour (ufo/track.py:40-139, ufo/sa.py:37-145, ufo/co.py:146-250,
+ufo/optics.py:44-238).  Instead of generating and building an OpenCL kernel
+in ``__init__`` they snapshot the line (element values are frozen at
+construction, as the reference's literals were) and in ``run()`` lower it
+with the current parameter values and call libufo_gb300.
+
+Arithmetic is FP64 whatever the flags say; DOUBLE_PRECISION only selects the
+dtype of ``parameters`` and of the outputs, as in the reference.  ``threads``
+is accepted and ignored: the kernels size their own grid.
+"""
+import copy
+
+import numpy as np
+
+from . import capi
+from . import compiler as C
+from .flags import FIVED, DOUBLE_PRECISION, LINEAR, ACHROMATIC, FMA, KICK
+
+COORDS = ('x', 'px', 'y', 'py', 'z', 'dp')
+
+_default_ctx = {}
+
+
+class Context(capi.Context):
+    """CUDA device handle; the reference's ``ufo.context(device)``."""
+
+
+def context(device=0):
+    """Return the (shared) context of ``device``."""
+    if device not in _default_ctx:
+        _default_ctx[device] = Context(device)
+    return _default_ctx[device]
+
+
+def list_devices(device=None):
+    """Print the CUDA devices, or return the id of ``device`` if given."""
+    import ctypes
+    lib = capi.load()
+    n = ctypes.c_int()
+    capi.check(lib.ufo_device_count(ctypes.byref(n)))
+    if device is not None:
+        if not 0 <= device < n.value:
+            raise ValueError(f'no CUDA device {device}')
+        return device
+    for i in range(n.value):
+        print(f'{i}:   CUDA device {i}')
+    return None
+
+
+def _ufloat(flags):
+    return np.float64 if flags & DOUBLE_PRECISION else np.float32
+
+
+def _snapshot(line):
+    """Frozen copy of the flattened line (the reference bakes element values
+    into its kernel at construction time)."""
+    from .lattice import Line
+    flat = line.flatten() if hasattr(line, 'flatten') else list(line)
+    return Line(getattr(line, 'label', 'line'), [copy.deepcopy(e) for e in flat])
+
+
+def _lattice_columns(parameters):
+    return [i for i, p in enumerate(parameters) if not (isinstance(p, str) and p in COORDS)]
+
+
+class _Compiled:
+    """Lowers the frozen line per run; re-uploads only what changed."""
+
+    def __init__(self, line, flags, parameters, where, count=None, dump_end=None):
+        self.line = line
+        self.flags = flags
+        self.parameters = list(parameters)
+        self.where = list(where)
+        self.count = count
+        self.dump_end = dump_end
+        self.lat_cols = _lattice_columns(self.parameters)
+        self._key = None
+        self._dprog = None
+        self._ops = None
+        self.prog = None
+        # compile once with zeros so that lowering errors surface in __init__
+        self.prog = C.compile_line(line, flags, self.parameters, self.where,
+                                   count=count, dump_end=dump_end)
+
+    def seeds(self, pool):
+        """Distinct lattice-parameter rows -> (seed_values, seed index per row)."""
+        n = pool.shape[0]
+        width = max(len(self.parameters), 1)
+        if not self.lat_cols:
+            return np.zeros((1, width)), None
+        lat = np.ascontiguousarray(pool[:, self.lat_cols], dtype=np.float64)
+        uniq, inv = np.unique(lat, axis=0, return_inverse=True)
+        vals = np.zeros((uniq.shape[0], width))
+        vals[:, self.lat_cols] = uniq
+        inv = inv.reshape(n).astype(np.int32)
+        if uniq.shape[0] == 1:
+            return vals, None
+        return vals, inv
+
+    def device(self, ctx, seed_values):
+        key = seed_values.tobytes()
+        if self._dprog is not None and key == self._key:
+            return self._dprog
+        prog = C.compile_line(self.line, self.flags, self.parameters, self.where, seed_values,
+                              count=self.count, dump_end=self.dump_end)
+        if self._dprog is not None and self._ops is not None and \
+                np.array_equal(prog.ops, self._ops) and \
+                prog.table.shape == (self._dprog.n_seeds, self._dprog.stride):
+            self._dprog.set_table(prog.table)
+        else:
+            self._dprog = capi.DeviceProgram(ctx, prog)
+            self._ops = prog.ops.copy()
+        self.prog = prog
+        self._key = key
+        return self._dprog
+
+
+def _coords_from_pool(pool, parameters, flags, dp):
+    n = pool.shape[0]
+    coords = np.zeros((n, 6))
+    for j, c in enumerate(COORDS):
+        if c in parameters:
+            coords[:, j] = pool[:, parameters.index(c)]
+    if flags & FIVED:
+        coords[:, 4] = 0.0
+        coords[:, 5] = dp
+    return coords
+
+
+def _track_flags(flags):
+    f = 0
+    if flags & FMA:
+        f |= capi.UFO_TRACK_FMA
+    if flags & FIVED:
+        f |= capi.UFO_TRACK_FIVED
+    return f
+
+
+class Track:
+    """Track a bunch through a ring, sampling coordinates at ``where`` every
+    turn (ufo/track.py:19-139).  Extensions: ``every`` samples only on every
+    ``every``-th turn (for long runs whose full record would not fit in host
+    memory); after ``run()``, ``lost`` holds the turn at which each particle
+    was lost (``turns`` if it survived) and ``final`` the last coordinates."""
+
+    def __init__(self, line, flags=0x00, turns=1000, particles=1000, parameters=None, where=None,
+                 dp=0., context=None, options=None, every=1):
+        parameters = list(parameters) if parameters is not None else []
+        where = where if where is not None else []
+        where = where if type(where) is list else [where]
+        self.turns = turns
+        self.ctx = context if context is not None else globals()['context'](0)
+        self.flags = flags
+        self.dp = dp
+        self.every = max(1, int(every))
+        ufloat = _ufloat(flags)
+        self.pool_idx = np.empty(1, np.int32)
+        self.parameters = np.zeros([particles, len(parameters)], dtype=ufloat)
+        self._names = parameters
+        self.count = len(where)
+        flat = line.flatten()
+        self.where = [(idx, flat[int(idx)]) for idx in where]
+        count = self.count * (turns // self.every)
+        if count < 1:
+            raise Exception("No valid observation points found in 'where'")
+        self._line = _snapshot(line)
+        self._c = _Compiled(self._line, flags, parameters, list(where))
+        self.tracks = np.zeros([particles, count, 6], dtype=ufloat)
+        self.lost = np.zeros(particles, dtype=np.uint32)
+        self.final = np.zeros([particles, 6], dtype=ufloat)
+        self.src = self._c.prog.describe()
+
+    @property
+    def program(self):
+        return self._c.prog
+
+    def run(self, threads=1):
+        """Track (synchronous).  ``threads`` is ignored."""
+        pool = np.asarray(self.parameters, dtype=np.float64)
+        seed_values, seed = self._c.seeds(pool)
+        dprog = self._c.device(self.ctx, seed_values)
+        coords = _coords_from_pool(pool, self._names, self.flags, self.dp)
+        slots = self.tracks.shape[1]
+        tracks, lost, final = capi.track(self.ctx, dprog, coords, self.turns,
+                                         capi.UFO_MODE_TRACK, _track_flags(self.flags),
+                                         seed=seed, slots=slots, every=self.every)
+        self.tracks = tracks.astype(self.tracks.dtype, copy=False)
+        self.lost = lost
+        self.final = final.astype(self.final.dtype, copy=False)
+
+
+class StableAperture:
+    """Turns survived per particle (ufo/sa.py:18-145): lost at the end of the
+    first turn with |x| > 1 or |y| > 1 or isnan(x); ``lost`` holds that turn,
+    or ``turns`` for survivors."""
+
+    def __init__(self, line, flags=0x00, turns=1000, particles=1000, parameters=None, dp=0.,
+                 context=None, options=None):
+        parameters = list(parameters) if parameters is not None else []
+        self.turns = turns
+        self.ctx = context if context is not None else globals()['context'](0)
+        self.flags = flags
+        self.dp = dp
+        ufloat = _ufloat(flags)
+        self.pool_idx = np.empty(1, np.int32)
+        self.parameters = np.zeros([particles, max(1, len(parameters))], dtype=ufloat)
+        self._names = parameters
+        self.lost = np.empty(particles, dtype=np.uint32)
+        self._line = _snapshot(line)
+        self._c = _Compiled(self._line, flags, parameters, [])
+        self.src = self._c.prog.describe()
+
+    @property
+    def program(self):
+        return self._c.prog
+
+    def run(self, threads=1):
+        pool = np.asarray(self.parameters, dtype=np.float64)
+        seed_values, seed = self._c.seeds(pool)
+        dprog = self._c.device(self.ctx, seed_values)
+        coords = _coords_from_pool(pool, self._names, self.flags, self.dp)
+        _, lost, final = capi.track(self.ctx, dprog, coords, self.turns, capi.UFO_MODE_SA,
+                                    _track_flags(self.flags), seed=seed, slots=0)
+        self.lost = lost
+        self.final = final
+
+
+class ClosedOrbit:
+    """Closed orbits (x, px, y, py) of the 4D one-turn map at dp = 0
+    (ufo/co.py:146-250).  The reference minimises the squared residual with a
+    fixed number of Nelder-Mead steps; this build solves F(z) = z by Newton
+    iteration, the Jacobian from the tangent map, until the step stops
+    shrinking (at most ``iterations`` steps)."""
+
+    def __init__(self, line, flags=0x00, particles=1000, parameters=None, dp=0., iterations=200,
+                 context=None, options=None):
+        parameters = list(parameters) if parameters is not None else []
+        self.ctx = context if context is not None else globals()['context'](0)
+        self.flags = flags
+        self.iterations = iterations
+        ufloat = _ufloat(flags)
+        self.pool_idx = np.empty(1, np.int32)
+        self.parameters = np.zeros([particles, max(1, len(parameters))], dtype=ufloat)
+        self._names = parameters
+        self.orbits = np.zeros([particles, 4], dtype=ufloat)
+        self._line = _snapshot(line)
+        # dp = 0, oodppo = 1, z = 0 are forced by the reference (ufo/co.py:182-184)
+        self._c = _Compiled(self._line, flags & ~FIVED, parameters, [])
+        self.src = self._c.prog.describe()
+
+    def run(self, threads=1):
+        from . import tangent
+        pool = np.asarray(self.parameters, dtype=np.float64)
+        seed_values, seed = self._c.seeds(pool)
+        dprog = self._c.device(self.ctx, seed_values)
+        guess = np.zeros((pool.shape[0], 4))
+        for j, c in enumerate(COORDS[:4]):
+            if c in self._names:
+                guess[:, j] = pool[:, self._names.index(c)]
+        orbits, self.residual = tangent.closed_orbit(self.ctx, dprog, guess, seed=seed,
+                                                     fma=bool(self.flags & FMA),
+                                                     max_iter=self.iterations)
+        self.orbits = orbits.astype(self.orbits.dtype, copy=False)
+
+
+class Optics:
+    """Periodic (or propagated) Twiss functions from the one-turn and partial
+    maps (ufo/optics.py:21-238): three unit particles (x=y=1), (px=py=1),
+    (dp=1) are tracked once with observations at ``where``; with the default
+    LINEAR | ACHROMATIC flags the map is linear so the tracks are the map's
+    columns.  Results: ``qx, qy, bx, by, ax, ay, dx, dpx, dy, dpy, mux, muy``."""
+
+    def __init__(self, line, where=None, periodic=True, parameters=None, flags=LINEAR | ACHROMATIC,
+                 context=None, options=None):
+        parameters = list(parameters) if parameters is not None else []
+        where = list(where) if where is not None else []
+        where = where if type(where) is list else [where]
+        self.ctx = context if context is not None else globals()['context'](0)
+        self.periodic = periodic
+        self.flags = flags
+        if periodic and -1 not in where and line[-1] not in where:
+            where.append(-1)
+        self.parameters = np.zeros([1, max(1, len(parameters))], dtype=_ufloat(flags))
+        self._names = parameters
+        self.count = len(where) - 1
+        if -1 in where:
+            self.count += 1
+        flat = line.flatten()
+        self.where = [(idx, flat[int(idx)]) for idx in where]
+        if self.count < 1:
+            raise Exception("No valid observation points found in 'where'")
+        self._line = _snapshot(line)
+        self._c = _Compiled(self._line, flags, parameters, where, count=self.count)
+        self.track = np.zeros([3, self.count, 6], dtype=_ufloat(flags))
+        self.src = self._c.prog.describe()
+        self.ax0 = self.bx0 = self.dx0 = self.dpx0 = 0.
+        self.ay0 = self.by0 = self.dy0 = self.dpy0 = 0.
+        for a in ('ax', 'ay', 'bx', 'by', 'dx', 'dy', 'dpx', 'dpy', 'mux', 'muy'):
+            setattr(self, a, np.empty(self.count))
+
+    def run(self, threads=3):
+        pool = np.asarray(self.parameters, dtype=np.float64)
+        seed_values, _ = self._c.seeds(pool[:1])
+        dprog = self._c.device(self.ctx, seed_values)
+        coords = np.zeros((3, 6))
+        coords[0, 0] = coords[0, 2] = 1.0
+        coords[1, 1] = coords[1, 3] = 1.0
+        coords[2, 5] = 1.0
+        if 'dp' in self._names:
+            coords[:, 5] += pool[0, self._names.index('dp')]
+        tracks, _, _ = capi.track(self.ctx, dprog, coords, 1, capi.UFO_MODE_TRACK,
+                                  _track_flags(self.flags & ~FIVED), slots=self.count)
+        tracks[:, :, 4:] = 0.0  # the reference's optics kernel dumps only x..py
+        self.track = tracks.astype(self.track.dtype, copy=False)
+        twiss(self)
+
+
+def twiss(o):
+    """Host Twiss/tune/dispersion from the unit tracks, the formulas of
+    ufo/optics.py:156-238."""
+    tr = np.asarray(o.track, dtype=np.float64)
+    if o.periodic:
+        re, im, dp = tr[0][-1], tr[1][-1], tr[2][-1]
+        cos_nu = (re[0] + im[1]) * 0.5
+        if np.absolute(cos_nu) > 1.:
+            o.ax0 = o.bx0 = o.qx = np.nan
+            return
+        o.bx0 = np.absolute(im[0] / np.sin(np.arccos(cos_nu)))
+        sin_nu = im[0] / o.bx0
+        nu = np.arctan2(sin_nu, cos_nu)
+        if nu < 0.:
+            nu += 2. * np.pi
+        o.ax0 = (re[0] - im[1]) / (2. * np.sin(nu))
+        o.qx = nu / (2. * np.pi)
+        k = 2. - re[0] - im[1]
+        o.dx0 = ((1. - im[1]) * dp[0] + im[0] * dp[1]) / k
+        o.dpx0 = ((1. - re[0]) * dp[1] + re[1] * dp[0]) / k
+        cos_nu = (re[2] + im[3]) * 0.5
+        if np.absolute(cos_nu) > 1.:
+            o.ay0 = o.by0 = o.qy = np.nan
+            return
+        o.by0 = np.absolute(im[2] / np.sin(np.arccos(cos_nu)))
+        sin_nu = im[2] / o.by0
+        nu = np.arctan2(sin_nu, cos_nu)
+        if nu < 0.:
+            nu += 2. * np.pi
+        o.ay0 = (re[2] - im[3]) / (2. * np.sin(nu))
+        o.qy = nu / (2. * np.pi)
+    for idx, (re, im, dp) in enumerate(zip(tr[0], tr[1], tr[2])):
+        gamma0 = (1. + o.ax0 * o.ax0) / o.bx0
+        o.ax[idx] = -re[0] * re[1] * o.bx0
+        o.ax[idx] += (re[0] * im[1] + im[0] * re[1]) * o.ax0
+        o.ax[idx] += -im[0] * im[1] * gamma0
+        o.bx[idx] = re[0] * re[0] * o.bx0
+        o.bx[idx] += -re[0] * im[0] * o.ax0 * 2.
+        o.bx[idx] += im[0] * im[0] * gamma0
+        o.dx[idx] = re[0] * o.dx0 + im[0] * o.dpx0 + dp[0]
+        o.dpx[idx] = re[1] * o.dx0 + im[1] * o.dpx0 + dp[1]
+        sin_mu = im[0] / np.sqrt(o.bx0 * o.bx[idx])
+        cos_mu = re[0] * np.sqrt(o.bx0 / o.bx[idx]) - o.ax0 * sin_mu
+        o.mux[idx] = np.arctan2(sin_mu, cos_mu)
+        gamma0 = (1. + o.ay0 * o.ay0) / o.by0
+        o.ay[idx] = -re[2] * re[3] * o.by0
+        o.ay[idx] += (re[2] * im[3] + im[2] * re[3]) * o.ay0
+        o.ay[idx] += -im[2] * im[3] * gamma0
+        o.by[idx] = re[2] * re[2] * o.by0
+        o.by[idx] += -re[2] * im[2] * o.ay0 * 2.
+        o.by[idx] += im[2] * im[2] * gamma0
+        o.dy[idx] = re[2] * o.dy0 + im[2] * o.dpy0 + dp[2]
+        o.dpy[idx] = re[3] * o.dy0 + im[3] * o.dpy0 + dp[3]
+        sin_mu = im[2] / np.sqrt(o.by0 * o.by[idx])
+        cos_mu = re[2] * np.sqrt(o.by0 / o.by[idx]) - o.ay0 * sin_mu
+        o.muy[idx] = np.arctan2(sin_mu, cos_mu)
+
+
+def chromaticity(optics):
+    """Analytic natural + sextupole chromaticity from Twiss at element starts
+    (the formulas of ufo/chroma.py:11-52).  Returns ((dqx0, dqy0), (dqx, dqy))."""
+    dqx0 = dqy0 = dqx = dqy = 0.
+    for (_, element), ax, ay, bx, by, dx, dpx in zip(optics.where, optics.ax, optics.ay,
+                                                     optics.bx, optics.by, optics.dx, optics.dpx):
+        l = getattr(element, 'length', 0.)
+        k = getattr(element, 'k1', 0.)
+        if l != 0 and k != 0:
+            k2 = np.sqrt(np.absolute(k))
+            k2l = l * k2
+            gx = (1. + ax * ax) / bx
+            gy = (1. + ay * ay) / by
+            S = np.sin(2. * k2l) / 4. / k2
+            SH = np.sinh(2. * k2l) / 4. / k2
+            Cc = (np.cos(k2l) ** 2 - 1.) / k2 / k2
+            CH = (np.cosh(k2l) ** 2 - 1.) / k2 / k2
+            if k > 0:
+                dqx0 -= (bx * (l / 2. + S) + ax * Cc + gx * (l / 2. - S) / k2 / k2) * k
+                dqy0 += (by * (l / 2. + SH) - ay * CH - gy * (l / 2. - SH) / k2 / k2) * k
+            else:
+                dqy0 += (by * (l / 2. + S) + ay * Cc + gy * (l / 2. - S) / k2 / k2) * k
+                dqx0 -= (bx * (l / 2. + SH) - ax * CH - gx * (l / 2. - SH) / k2 / k2) * k
+        k = getattr(element, 'k2', 0.)
+        if l != 0 and k != 0:
+            gx = (1. + ax * ax) / bx
+            gy = (1. + ay * ay) / by
+            dqx += (dx * (bx + (gx * l / 3. - ax) * l) + dpx * l *
+                    (bx / 2. - l * (2. * ax / 3. + gx * l / 4.))) * l * k
+            dqy -= (dx * (by + (gy * l / 3. - ay) * l) + dpx * l *
+                    (by / 2. - l * (2. * ay / 3. + gy * l / 4.))) * l * k
+    dqx0 /= 4. * np.pi
+    dqy0 /= 4. * np.pi
+    dqx /= 4. * np.pi
+    dqy /= 4. * np.pi
+    dqx += dqx0
+    dqy += dqy0
+    return (dqx0, dqy0), (dqx, dqy)
