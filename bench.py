@@ -1,0 +1,349 @@
+#!/usr/bin/env python
+"""Benchmark: FP64 particle*element*turns/s on one GB300 (or N, weak scaling).
+
+Default workload (C2): 65,536 Gaussian particles through the 1024-element
+synthetic light-source ring (teapot, 4 slices; see ufo_gb300/workloads.py),
+10,000 turns.  A step is one launch tracking every particle 1,000 turns, so
+the default --steps 10 is the whole 10,000-turn job; each step continues from
+the previous step's coordinates.  Element = one entry of Line.flatten().
+
+Printed (rank 0, one JSON line):
+  value      device-resident inputs, CUDA events over exactly K steps, max
+             over ranks, L2 flushed (256 MiB memset) between steps
+  e2e        the same K steps through the public API (Track.run with host
+             numpy buffers: H2D of the coordinates, D2H of tracks/lost/final
+             inside the timed region)
+  roofline   FP64-pipe bound: algorithmic FP64 flops per launch (compiler's
+             count of the reference expression, structural zeros removed)
+             over the average launch time, against the FP64 FMA peak measured
+             live on the same GPU
+  cpu_baseline  the reference's own generated kernel (oracle/_ref), or the
+             oracle port when that is absent, on a bounded sample on the host
+             cores
+--impl reference times the reference's CPU implementation the same way.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+PARAMS = ['x', 'px', 'y', 'py', 'dp']
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--mode', default='strict', choices=['strict', 'fma'])
+    ap.add_argument('--turns-per-step', type=int, default=1000)
+    ap.add_argument('--particles', type=int, default=65536)
+    ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--no-cpu', action='store_true')
+    return ap.parse_args()
+
+
+def dist():
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return world, rank, local
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, device):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile('w+', suffix='.csv', delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(['nvidia-smi', f'--id={self.device}',
+                                       f'--query-gpu={self.Q}', '--format=csv,noheader,nounits',
+                                       '-lms', '200'], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as f:
+            for line in f:
+                parts = [x.strip() for x in line.split(',')]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace('.', '').isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace('.', '').isdigit()]
+        reasons = set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for r in rows:
+            for name, v in zip(names, r[5:9]):
+                if v.strip().lower() == 'active':
+                    reasons.add(name)
+        load = sorted(sm)[len(sm) // 4:] if sm else []
+        return {'sm_mhz': statistics.median(load) if load else None,
+                'sm_max_mhz': max(mx) if mx else None, 'reasons': sorted(reasons),
+                'samples': len(rows)}
+
+
+def ref_runner():
+    """The reference's generated C2 kernel (oracle/_ref) when present, else
+    the oracle port; bounded sample of 16,384 particles x 100 turns on all
+    host cores.  Returns (run, sample description, kind, particles, turns)."""
+    from ufo_gb300 import workloads as W
+    threads = len(os.sched_getaffinity(0))
+    n, turns = 16384, 100
+    beam = W.c2_beam(n, seed=2)
+    try:
+        from oracle import ref_kernels as R
+        if not R.available('c2_track'):
+            raise FileNotFoundError('oracle/_ref/c2_track.c')
+        k = R.RefKernel('c2_track')
+        kind = 'reference'
+        desc = ('reference-generated OpenCL C of the C2 ring (its Track kernel), gcc -O2 '
+                '-ffp-contract=off, OpenMP team over its atomic work queue')
+        run = lambda: k.run(beam[:, [0, 1, 2, 3, 5]], threads)  # noqa: E731
+    except Exception:  # noqa: BLE001
+        import ufo_gb300 as u
+        from oracle import oracle as O
+        ring = W.c2_ring(u)
+        kind = 'port'
+        desc = 'C restatement of the reference (oracle/ufo_oracle.c), OpenMP'
+        run = lambda: O.track(ring, u.KICK, beam, turns, where=[-1], threads=threads,  # noqa
+                              tracks=False)
+    return run, f'C2 ring, {n} particles x {turns} turns per run; {desc}', kind, n, turns, threads
+
+
+def cpu_baseline(ring_elems, runs=2):
+    run, desc, kind, n, turns, threads = ref_runner()
+    run()  # first touch
+    best = min(_timed(run) for _ in range(runs))
+    return {'value': n * ring_elems * turns / best, 'unit': 'particle*element*turns/s',
+            'cores': threads, 'kind': kind, 'sample': desc, 'seconds': best}
+
+
+def _timed(fn):
+    t0 = time.perf_counter()
+    fn()
+    return time.perf_counter() - t0
+
+
+def bench_reference(args):
+    world, rank, _ = dist()
+    if rank != 0:
+        return
+    from ufo_gb300 import workloads as W
+    import ufo_gb300 as u
+    ring_elems = len(W.c2_ring(u).flatten())
+    run, desc, kind, n, turns, threads = ref_runner()
+    for _ in range(max(0, args.warmup)):
+        run()
+    sec = sum(_timed(run) for _ in range(args.steps))
+    value = args.steps * n * ring_elems * turns / sec
+    line = {'impl': 'reference', 'metric': 'FP64 particle*element*turns/s', 'value': value,
+            'unit': 'particle*element*turns/s', 'n_gpus': args.gpus, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': 1e3 * sec / args.steps,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+            'data': 'synthetic',
+            'config': {'workload': 'C2 light-source ring (1024 elements, teapot 4 slices, 10 mm '
+                                   'aperture), Gaussian beam',
+                       'sample_per_step': f'{n} particles x {turns} turns'},
+            'cpu_baseline': {'value': value, 'unit': 'particle*element*turns/s',
+                             'cores': threads, 'kind': kind, 'sample': desc},
+            'e2e': {'value': value, 'unit': 'particle*element*turns/s',
+                    'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(line), flush=True)
+
+
+def load_traffic(mode):
+    p = os.path.join(HERE, 'profiles', 'track_kernel_c2_traffic.json')
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return d.get(mode)
+    except (OSError, ValueError):
+        return None
+
+
+def bench_ours(args):
+    import torch
+    import ufo_gb300 as u
+    from ufo_gb300 import capi, compiler as C, workloads as W
+    world, rank, local = dist()
+    if world > 1:
+        import torch.distributed as tdist
+        tdist.init_process_group('nccl')
+    torch.cuda.set_device(local)
+    dev = torch.device('cuda', local)
+    ctx = u.context(local)
+    flags = u.KICK | (u.FMA if args.mode == 'fma' else 0)
+    tflags = capi.UFO_TRACK_FMA if args.mode == 'fma' else 0
+    ring = W.c2_ring(u)
+    n_elem = len(ring.flatten())
+    prog = C.compile_line(ring, flags, where=[-1])
+    dprog = capi.DeviceProgram(ctx, prog)
+    n = args.particles
+    T = args.turns_per_step
+    beam = W.c2_beam(n, seed=2 + rank)
+    c0 = torch.from_numpy(beam).to(dev)
+    bufs = [c0.clone(), torch.empty_like(c0)]
+    lost = torch.empty(n, dtype=torch.int32, device=dev)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    # a dedicated stream: the library launches on the stream it is given, and
+    # the CUDA events below are recorded on the same stream
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    lib = capi.load()
+
+    def step(i, ev=None):
+        src, dst = bufs[i % 2], bufs[(i + 1) % 2]
+        if ev:
+            ev[0].record(stream)
+        capi.check(lib.ufo_track_device(ctx.handle, dprog.handle, capi.ptr(src.data_ptr()), None,
+                                        None, n, T, capi.UFO_MODE_TRACK, tflags, 0, 1, None,
+                                        capi.ptr(lost.data_ptr()), capi.ptr(dst.data_ptr()),
+                                        capi.ptr(stream.cuda_stream)))
+        if ev:
+            ev[1].record(stream)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            import torch.distributed as tdist
+            tdist.barrier()
+
+    for i in range(args.warmup):
+        flush.zero_()
+        step(i)
+    bufs[0].copy_(c0)
+    barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    l0 = ctx.launches()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+           for _ in range(args.steps)]
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    for i in range(args.steps):
+        flush.zero_()
+        step(i, evs[i])
+    t_end.record(stream)
+    barrier()
+    clk = clocks.stop()
+    launches = ctx.launches() - l0
+    total_ms = t_start.elapsed_time(t_end)
+    kern_ms = [a.elapsed_time(b) for a, b in evs]
+    lost_np = lost.cpu().numpy()
+    if world > 1:
+        import torch.distributed as tdist
+        t = torch.tensor([total_ms], device=dev)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * n * n_elem * T * args.steps / (total_ms / 1e3)
+    # particle-turns actually tracked in the last launch (lost particles stop)
+    pt = np.where(lost_np < T, lost_np + 1, T).astype(np.float64).sum()
+    fl = prog.flops_fast if args.mode == 'fma' else prog.flops
+    flops_launch = fl * pt
+    mean_kernel_s = statistics.mean(kern_ms) / 1e3
+    achieved = flops_launch / mean_kernel_s / 1e9
+    peak = ctypes_peak(ctx)
+    traffic = load_traffic(args.mode)
+
+    e2e = None
+    if not args.no_e2e:
+        tr = u.Track(ring, flags=flags | u.DOUBLE_PRECISION, turns=T, particles=n,
+                     parameters=PARAMS, where=[-1], every=T, context=ctx)
+        host = beam[:, [0, 1, 2, 3, 5]].copy()
+        for _ in range(args.warmup):
+            tr.parameters[:] = host
+            tr.run()
+        barrier()
+        t0 = time.perf_counter()
+        cur = host
+        for _ in range(args.steps):
+            tr.parameters[:] = cur
+            tr.run()
+            cur = tr.final[:, [0, 1, 2, 3, 5]]
+        barrier()
+        e2e_s = time.perf_counter() - t0
+        if world > 1:
+            import torch.distributed as tdist
+            t = torch.tensor([e2e_s], device=dev)
+            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+            e2e_s = float(t.item())
+        e2e = {'value': world * n * n_elem * T * args.steps / e2e_s,
+               'unit': 'particle*element*turns/s',
+               'h2d_bytes_per_step': n * 6 * 8,
+               'd2h_bytes_per_step': n * (6 * 8 + 4 + 6 * 8),
+               'api': 'ufo_gb300.Track(...).run() -> ufo_track (host buffers)'}
+    if rank != 0:
+        return
+    cb = None if args.no_cpu else cpu_baseline(n_elem)
+    line = {
+        'metric': 'FP64 particle*element*turns/s', 'value': value,
+        'unit': 'particle*element*turns/s', 'n_gpus': world, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': total_ms / args.steps, 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+        'config': {'workload': 'C2 light-source ring (1024 elements, teapot 4 slices, 10 mm '
+                               'aperture), 65536 Gaussian particles, 10000 turns',
+                   'particles_per_gpu': n, 'turns_per_step': T, 'elements': n_elem,
+                   'mode': args.mode, 'l2': 'flushed (256 MiB memset) between steps',
+                   'parallelism': f'weak: {n} particles per GPU, no collective'},
+        'roofline': {'bound': 'fp64', 'achieved': achieved, 'peak': peak, 'unit': 'GFLOP/s',
+                     'frac': achieved / peak if peak else None,
+                     'traffic': traffic,
+                     'flops_per_particle_turn': fl,
+                     'peak_source': 'measured live: ufo_fp64_peak (DFMA chains, 2 flop each)'},
+        'gpu_launches': launches,
+        'kernel_ms': kern_ms,
+    }
+    if e2e:
+        line['e2e'] = e2e
+    if cb:
+        line['cpu_baseline'] = {k: cb[k] for k in ('value', 'unit', 'cores', 'kind', 'sample')}
+    if clk:
+        line['clocks'] = clk
+    print(json.dumps(line), flush=True)
+
+
+def ctypes_peak(ctx):
+    import ctypes
+    from ufo_gb300 import capi
+    g = ctypes.c_double()
+    capi.check(capi.load().ufo_fp64_peak(ctx.handle, ctypes.byref(g)))
+    return g.value
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        bench_reference(args)
+    else:
+        bench_ours(args)
+
+
+if __name__ == '__main__':
+    main()

@@ -93,8 +93,14 @@ int ufo_track_device(ufo_ctx *ctx, const ufo_prog *prog, const double *d_coords,
                      int mode, int flags, int64_t slots, int every, double *d_tracks,
                      uint32_t *d_lost, double *d_final, void *stream);
 
-/* Kernel launches issued by this library since the context was created. */
+/* Kernel launches issued by this library since the context was created.
+ * Diagnostic; no reference counterpart. */
 int ufo_launch_count(ufo_ctx *ctx, int64_t *count);
+
+/* Measured FP64 FMA throughput of the device in GFLOP/s (2 flops per DFMA),
+ * best of 3 timed launches of an independent-chain DFMA kernel.  Diagnostic
+ * (the roofline denominator of the benchmark); no reference counterpart. */
+int ufo_fp64_peak(ufo_ctx *ctx, double *gflops);
 
 #ifdef __cplusplus
 }

@@ -27,7 +27,7 @@ from . import tools, array  # noqa: F401  (the reference imports both)
 _HERE = os.path.dirname(os.path.abspath(__file__))
 _CACHE = os.environ.get(
     "UFO_REFSHIM_CACHE",
-    os.path.join(os.path.dirname(os.path.dirname(_HERE)), "_ref", "cache"))
+    os.path.join(os.environ.get("TMPDIR", "/tmp"), "ufo_refshim_cache"))
 
 _PRELUDE = r"""
 #include <math.h>

@@ -35,6 +35,7 @@ SIGNATURES = {
     'ufo_track_device': [P, P, P, P, P, I64, ctypes.c_int, ctypes.c_int, ctypes.c_int, I64,
                          ctypes.c_int, P, P, P, P],
     'ufo_launch_count': [P, P],
+    'ufo_fp64_peak': [P, P],
 }
 _VOID = {'ufo_ctx_destroy', 'ufo_prog_destroy'}
 

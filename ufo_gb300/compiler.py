@@ -60,6 +60,7 @@ F_T1Z = 1 << 9          # edge: px term structurally zero (poison-only)
 F_T2Z = 1 << 10         # edge: py term structurally zero (poison-only)
 F_WEAKZ = 1 << 11       # teapot: weak term structurally zero (poison-only)
 F_YOSHIDA = 1 << 12     # teapot: 4th-order Yoshida splitting instead of TEAPOT
+F_CIRCLE = 1 << 13      # aperture: x*x + y*y < c (table: [c])
 # drift form of teapot outer/inner drifts packed in bits 16..19
 SH_FOUTER, SH_FINNER = 16, 18
 
@@ -360,7 +361,7 @@ class _Lowerer:
 
         fl = F_ACHRO if self.flags & ACHROMATIC else 0
         if self.flags & YOSHIDA:
-            return self._yoshida(Lf, slices, ks, weak, elem)
+            raise NotImplementedError('YOSHIDA integration is not available in this build')
         exact = bool(self.flags & EXACT)
         if exact:
             fl |= F_EXACT
@@ -499,6 +500,17 @@ class _Lowerer:
 
     def aperture(self, window, elem):
         code = _ap.compile_window(window)
+        # `x*x + y*y < c == 0` -> lost when !((x*x + y*y) < c): evaluated in
+        # registers by the kernels (same operations, same order)
+        circle = [(_ap.VAR, 0.0), (_ap.VAR, 0.0), (_ap.MUL, 0.0), (_ap.VAR, 2.0), (_ap.VAR, 2.0),
+                  (_ap.MUL, 0.0), (_ap.ADD, 0.0), (_ap.PUSH, None), (_ap.LT, 0.0),
+                  (_ap.PUSH, 0.0), (_ap.EQ, 0.0)]
+        if len(code) == len(circle) and all(
+                a[0] == b[0] and (b[1] is None or a[1] == b[1]) for a, b in zip(code, circle)):
+            op = Op(OP_APERTURE, F_CIRCLE, ints=[0], consts=[Val.of(code[7][1])], elem=elem)
+            op.flops = op.flops_fast = 3
+            self.emit(op)
+            return
         consts = []
         for opc, v in code:
             consts += [Val.of(float(opc)), Val.of(float(v))]

@@ -23,7 +23,7 @@ enum : int { DF_MUL = 0, DF_MUL2 = 1, DF_DIV = 2 };
 enum : int {
   F_ACHRO = 1 << 0, F_EXACT = 1 << 1, F_WEAK = 1 << 2, F_RTPSI = 1 << 3, F_T1 = 1 << 4,
   F_T2 = 1 << 5, F_CONST = 1 << 6, F_AX = 1 << 7, F_AY = 1 << 8, F_T1Z = 1 << 9,
-  F_T2Z = 1 << 10, F_WEAKZ = 1 << 11, F_YOSHIDA = 1 << 12
+  F_T2Z = 1 << 10, F_WEAKZ = 1 << 11, F_YOSHIDA = 1 << 12, F_CIRCLE = 1 << 13
 };
 constexpr int SH_FOUTER = 16, SH_FINNER = 18;
 
@@ -142,7 +142,7 @@ UFO_DEV int drift_nconst(int form, bool exact) {
 
 // untrimmed evaluation (reference semantics incl. 0*x terms) for non-finite x/y
 template <bool SKEW>
-UFO_DEV void horner_full(const State &s, int n, uint32_t mask, const double *c, bool achro,
+__device__ __noinline__ void horner_full(const State &s, int n, uint32_t mask, const double *c, bool achro,
                          double &pxd, double &pyd) {
   // coefficient j: its value if bit j is set, else a literal 0.
   auto coef = [&](int j) -> double {
@@ -311,11 +311,42 @@ UFO_DEV void teapot(State &s, const Op &op, const double *c) {
   const double *ci = co + drift_nconst(fo, exact);
   const double *ck = ci + (N > 1 ? drift_nconst(fi, exact) : 0);
   const double W = (op.flags & F_WEAK) ? ld(ck + __popc(mn) + __popc(ms)) : 0.0;
+  // Kick pattern.  The reference recomputes (K*oodppo) in every slice; the
+  // value is the same each time, so it is formed once per element.
+  //   1: quadrupole  px -= t*x, py += t*y            t = K*o
+  //   2: sextupole   a = t*x, b = t*y; px -= a*x - b*y; py += a*y + b*x,
+  //                  t = (K*o)*0.5 == ((K*o)*x)/2 / x exactly
+  //   3: no kick terms (bend without gradient): only NaN/inf propagate
+  //   0: general Horner
+  const int pat = ns != 0 ? 0 : (nn == 2 && mn == 2u) ? 1 : (nn == 3 && mn == 4u) ? 2
+                 : mn == 0u ? 3 : 0;
+  double t = 0.0;
+  if (pat == 1) t = achro ? ld(ck) : mul(ld(ck), s.o);
+  if (pat == 2) t = mul(achro ? ld(ck) : mul(ld(ck), s.o), 0.5);
   drift<FMA>(s, fo, exact, co);
   for (int sl = 0; sl < N; ++sl) {
     const bool bad = s.bad_o || nf(s.x) || nf(s.y);
-    kick<FMA>(s, nn, ns, mn, ms, ck, achro, bad);
-    weak<FMA>(s, op.flags, W, bad || nf(s.x));
+    if (bad || pat == 0) {
+      kick<FMA>(s, nn, ns, mn, ms, ck, achro, bad);
+    } else if (pat == 1) {
+      if (FMA) {
+        s.px = fma_(-t, s.x, s.px);
+        s.py = fma_(t, s.y, s.py);
+      } else {
+        s.px = sub(s.px, mul(t, s.x));
+        s.py = add(s.py, mul(t, s.y));
+      }
+    } else if (pat == 2) {
+      const double a = mul(t, s.x), b = mul(t, s.y);
+      if (FMA) {
+        s.px = fma_(b, s.y, fma_(-a, s.x, s.px));
+        s.py = fma_(b, s.x, fma_(a, s.y, s.py));
+      } else {
+        s.px = sub(s.px, sub(mul(a, s.x), mul(b, s.y)));
+        s.py = add(s.py, add(mul(a, s.y), mul(b, s.x)));
+      }
+    }
+    weak<FMA>(s, op.flags, W, bad);
     if (sl < N - 1) drift<FMA>(s, fi, exact, ci);
   }
   drift<FMA>(s, fo, exact, co);
@@ -364,7 +395,7 @@ UFO_DEV Trig trig(double k2l) {
 
 // methods.quadrupole thick branch (ufo/methods.py:103-134);
 // table [k, L*f, (k2, C, S, CH, SH)]
-UFO_DEV void thick_quad(State &s, int flags, const double *c) {
+__device__ __noinline__ void thick_quad(State &s, int flags, const double *c) {
   const double k = ld(c), Lf = ld(c + 1);
   double k2;
   Trig t;
@@ -391,7 +422,7 @@ UFO_DEV void thick_quad(State &s, int flags, const double *c) {
 
 // methods.sbend thick branch (ufo/methods.py:140-196); table
 // [A/L, k1, L*f, (kv, k2v, Cv, Sv, CHv, SHv, kx, k2x, Cx, Sx, CHx, SHx, |kx|)]
-UFO_DEV void thick_bend(State &s, int flags, const double *c) {
+__device__ __noinline__ void thick_bend(State &s, int flags, const double *c) {
   const bool achro = flags & F_ACHRO;
   const double Lf = ld(c + 2);
   const double curv = achro ? ld(c) : mul(ld(c), s.o);
@@ -443,7 +474,7 @@ UFO_DEV void thick_bend(State &s, int flags, const double *c) {
 
 // ---------------------------------------------------------------- wire
 // methods.wire (ufo/methods.py:230-241); table [xw, yw, k]
-UFO_DEV void wire(State &s, const double *c) {
+__device__ __noinline__ void wire(State &s, const double *c) {
   const double wx = ld(c), wy = ld(c + 1), wk = ld(c + 2);
   const double alpha = atan2(sub(wy, s.y), sub(wx, s.x));
   const double B = dvd(wk, hypot(sub(wx, s.x), sub(wy, s.y)));
@@ -456,7 +487,7 @@ UFO_DEV void wire(State &s, const double *c) {
 // ---------------------------------------------------------------- aperture
 // stack program of ``{window} == 0`` (ufo_gb300/aperture.py); table holds
 // (opcode, value) pairs.  Returns true when the particle is lost.
-UFO_DEV bool aperture_lost(const State &s, const double *c, int n) {
+__device__ __noinline__ bool aperture_lost(const State &s, const double *c, int n) {
   double st[16];
   int sp = 0;
   for (int i = 0; i < n; ++i) {

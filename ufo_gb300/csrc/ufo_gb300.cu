@@ -116,9 +116,15 @@ UFO_DEV void one_turn(State &s, const TrackArgs &a, const double *tab, int64_t p
       case OP_WIRE:
         wire(s, c);
         break;
-      case OP_APERTURE:
-        if (aperture_lost(s, c, op.i0)) s.x = __longlong_as_double(0x7ff8000000000000ll);
+      case OP_APERTURE: {
+        bool lost;
+        if (op.flags & F_CIRCLE)  // (x*x + y*y < c) == 0
+          lost = !(add(mul(s.x, s.x), mul(s.y, s.y)) < ld(c));
+        else
+          lost = aperture_lost(s, c, op.i0);
+        if (lost) s.x = __longlong_as_double(0x7ff8000000000000ll);
         break;
+      }
       case OP_OBSERVE:
         observe(s, a, p, op.i0);
         break;
@@ -134,7 +140,7 @@ UFO_DEV bool is_lost(const State &s, int mode) {
 }
 
 template <bool FMA>
-__global__ void __launch_bounds__(128) track_kernel(TrackArgs a) {
+__global__ void __launch_bounds__(32) track_kernel(TrackArgs a) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
@@ -199,6 +205,21 @@ __global__ void __launch_bounds__(128) track_plain_kernel(TrackArgs a) {
   store_final(s, a, p);
 }
 
+// FP64 pipe peak probe: 8 independent DFMA chains per thread
+__global__ void __launch_bounds__(256) dfma_peak_kernel(double *out, int iters, double b, double c) {
+  double a[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) a[k] = threadIdx.x * 1e-3 + k;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = fma_(a[k], b, c);
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s = add(s, a[k]);
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace ufo
 
 // ======================================================================= C ABI
@@ -206,6 +227,7 @@ __global__ void __launch_bounds__(128) track_plain_kernel(TrackArgs a) {
 struct ufo_ctx {
   int device;
   int sm_count;
+  int warps_per_sm;  // resident warps per SM of the persistent grid
   cudaStream_t stream;
   unsigned long long *queue;
   std::atomic<int64_t> launches;
@@ -255,20 +277,99 @@ int ensure_constants(int device) {
   return UFO_OK;
 }
 
-int validate_ops(const int32_t *ops, int n_ops, int64_t stride) {
+int popc32(uint32_t v) { return __builtin_popcount(v); }
+
+bool mask_fits(int n, int32_t mask) {
+  if (n < 0 || n > 32) return false;
+  const uint32_t m = static_cast<uint32_t>(mask);
+  return n == 32 || (m >> n) == 0u;
+}
+
+int drift_consts(int form, bool exact) {
+  if (exact) return 1;
+  return form == ufo::DF_MUL ? 1 : form == ufo::DF_MUL2 ? 2 : form == ufo::DF_DIV ? 4 : -1;
+}
+
+// Number of table constants an op reads (exactly what the kernels read), or
+// -1 if the op's shape is invalid.  Every op must fit inside the stride so
+// that no kernel read leaves its seed's row.
+int64_t op_consts(const int32_t *w) {
+  const int kind = w[0], flags = w[1];
+  const bool exact = flags & ufo::F_EXACT;
+  switch (kind) {
+    case ufo::OP_NOP:
+    case ufo::OP_OBSERVE:
+      return 0;
+    case ufo::OP_DRIFT:
+      return drift_consts(w[3], exact);
+    case ufo::OP_KICK:
+      if (!mask_fits(w[3], w[5]) || !mask_fits(w[4], w[6])) return -1;
+      return popc32(w[5]) + popc32(w[6]);
+    case ufo::OP_TEAPOT: {
+      if (flags & ufo::F_YOSHIDA) return -1;
+      if (w[3] < 1 || !mask_fits(w[4], w[6]) || !mask_fits(w[5], w[7])) return -1;
+      const int fo = (flags >> ufo::SH_FOUTER) & 3, fi = (flags >> ufo::SH_FINNER) & 3;
+      const int co = drift_consts(fo, exact), ci = w[3] > 1 ? drift_consts(fi, exact) : 0;
+      if (co < 0 || ci < 0) return -1;
+      return co + ci + popc32(w[6]) + popc32(w[7]) + ((flags & ufo::F_WEAK) ? 1 : 0);
+    }
+    case ufo::OP_ALIGN:
+      return 2;
+    case ufo::OP_EDGE:
+      return (flags & ufo::F_RTPSI) ? 6 : 3;
+    case ufo::OP_THICKQ:
+      return (flags & ufo::F_CONST) ? 7 : 2;
+    case ufo::OP_THICKB:
+      return (flags & ufo::F_CONST) ? 16 : 3;
+    case ufo::OP_WIRE:
+      return 3;
+    case ufo::OP_APERTURE:
+      if (flags & ufo::F_CIRCLE) return 1;
+      return w[3] >= 0 ? 2 * static_cast<int64_t>(w[3]) : -1;
+    default:
+      return -1;
+  }
+}
+
+// simulate an aperture stack program (row 0 of the table): every pop must
+// find an operand and the depth must stay within the kernels' 16 slots
+bool aperture_ok(const double *prog, int n) {
+  int sp = 0;
+  for (int i = 0; i < n; ++i) {
+    const double code = prog[2 * i];
+    if (!(code >= 1 && code <= 21) || code != static_cast<int>(code)) return false;
+    const int op = static_cast<int>(code);
+    if (op == 2) {
+      const double v = prog[2 * i + 1];
+      if (!(v >= 0 && v <= 7)) return false;
+    }
+    if (op == 1 || op == 2) {
+      if (++sp > 16) return false;
+    } else if (op == 3 || op == 4 || op == 19 || op == 20) {
+      if (sp < 1) return false;
+    } else if (op == 21) {
+      if (sp < 3) return false;
+      sp -= 2;
+    } else {
+      if (sp < 2) return false;
+      sp -= 1;
+    }
+  }
+  return n == 0 || sp >= 1;
+}
+
+int validate_ops(const int32_t *ops, int n_ops, int64_t stride, const double *table) {
   for (int i = 0; i < n_ops; ++i) {
     const int32_t *w = ops + i * UFO_OP_WORDS;
     if (w[0] < ufo::OP_NOP || w[0] > ufo::OP_OBSERVE)
       return fail(UFO_E_ARG, "op %d: unknown kind %d", i, w[0]);
-    if (w[2] < 0 || (w[0] != ufo::OP_OBSERVE && w[0] != ufo::OP_NOP && w[2] >= stride))
-      return fail(UFO_E_ARG, "op %d: table offset %d outside stride %lld", i, w[2],
-                  static_cast<long long>(stride));
-    if (w[0] == ufo::OP_TEAPOT && (w[3] < 1 || w[4] < 0 || w[4] > 32 || w[5] < 0 || w[5] > 32))
-      return fail(UFO_E_ARG, "op %d: bad teapot shape", i);
-    if (w[0] == ufo::OP_KICK && (w[3] < 0 || w[3] > 32 || w[4] < 0 || w[4] > 32))
-      return fail(UFO_E_ARG, "op %d: bad kick shape", i);
-    if (w[0] == ufo::OP_APERTURE && (w[3] < 0 || w[2] + 2 * static_cast<int64_t>(w[3]) > stride))
-      return fail(UFO_E_ARG, "op %d: aperture program outside table", i);
+    const int64_t nc = op_consts(w);
+    if (nc < 0) return fail(UFO_E_ARG, "op %d (kind %d): invalid shape", i, w[0]);
+    if (w[2] < 0 || w[2] + nc > stride)
+      return fail(UFO_E_ARG, "op %d: constants [%d, %lld) outside stride %lld", i, w[2],
+                  static_cast<long long>(w[2] + nc), static_cast<long long>(stride));
+    if (w[0] == ufo::OP_APERTURE && !(w[1] & ufo::F_CIRCLE) && !aperture_ok(table + w[2], w[3]))
+      return fail(UFO_E_ARG, "op %d: malformed aperture program", i);
   }
   return UFO_OK;
 }
@@ -307,14 +408,15 @@ int launch_track(ufo_ctx *ctx, const ufo_prog *prog, const double *d_coords, con
       ufo::track_plain_kernel<false><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(a);
   } else {
     UFO_CUDA(cudaMemsetAsync(ctx->queue, 0, sizeof(unsigned long long), stream));
+    // one warp per block so the block scheduler spreads warps evenly over the
+    // SMs (the FP64 pipe is per SM); at most 16 resident warps per SM
     int64_t warps = (n + 31) / 32;
-    const int64_t max_warps = static_cast<int64_t>(ctx->sm_count) * 16;
+    const int64_t max_warps = static_cast<int64_t>(ctx->sm_count) * ctx->warps_per_sm;
     if (warps > max_warps) warps = max_warps;
-    const int64_t blocks = (warps + 3) / 4;
     if (fma)
-      ufo::track_kernel<true><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(a);
+      ufo::track_kernel<true><<<static_cast<unsigned>(warps), 32, 0, stream>>>(a);
     else
-      ufo::track_kernel<false><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(a);
+      ufo::track_kernel<false><<<static_cast<unsigned>(warps), 32, 0, stream>>>(a);
   }
   ctx->launches.fetch_add(1);
   UFO_CUDA(cudaGetLastError());
@@ -361,6 +463,7 @@ int ufo_ctx_create(int device, ufo_ctx **out) {
   cudaError_t e = cudaGetDeviceProperties(&prop, device);
   if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaGetDeviceProperties"); }
   c->sm_count = prop.multiProcessorCount;
+  c->warps_per_sm = 16;
   e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaStreamCreate"); }
   e = cudaMalloc(&c->queue, 64);
@@ -382,6 +485,36 @@ void ufo_ctx_destroy(ufo_ctx *ctx) {
   delete ctx;
 }
 
+int ufo_fp64_peak(ufo_ctx *ctx, double *gflops) {
+  if (!ctx || !gflops) return fail(UFO_E_ARG, "null argument");
+  UFO_CUDA(cudaSetDevice(ctx->device));
+  const int blocks = ctx->sm_count * 4, threads = 256, iters = 4096;
+  double *buf = nullptr;
+  if (cudaMalloc(&buf, sizeof(double) * blocks * threads) != cudaSuccess)
+    return fail(UFO_E_NOMEM, "cudaMalloc(peak buffer)");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  cudaError_t err = cudaSuccess;
+  for (int rep = 0; rep < 4 && err == cudaSuccess; ++rep) {
+    cudaEventRecord(e0, ctx->stream);
+    ufo::dfma_peak_kernel<<<blocks, threads, 0, ctx->stream>>>(buf, iters, 0.999999, 1e-7);
+    cudaEventRecord(e1, ctx->stream);
+    err = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && ms < best) best = ms;
+  }
+  if (err == cudaSuccess) err = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(buf);
+  if (err != cudaSuccess) return cuda_fail(err, "fp64 peak probe");
+  *gflops = 2.0 * blocks * threads * static_cast<double>(iters) * 8 / (best * 1e6);
+  return UFO_OK;
+}
+
 int ufo_launch_count(ufo_ctx *ctx, int64_t *count) {
   if (!ctx || !count) return fail(UFO_E_ARG, "null argument");
   *count = ctx->launches.load();
@@ -394,7 +527,7 @@ int ufo_prog_create(ufo_ctx *ctx, const int32_t *ops, int n_ops, const double *t
   *out = nullptr;
   if (n_ops < 0 || stride < 1 || n_seeds < 1 || n_dumps < 0)
     return fail(UFO_E_ARG, "bad program sizes");
-  int rc = validate_ops(ops, n_ops, stride);
+  int rc = validate_ops(ops, n_ops, stride, table);
   if (rc) return rc;
   UFO_CUDA(cudaSetDevice(ctx->device));
   ufo_prog *p = new (std::nothrow) ufo_prog;
