@@ -142,7 +142,7 @@ UFO_DEV int drift_nconst(int form, bool exact) {
 
 // untrimmed evaluation (reference semantics incl. 0*x terms) for non-finite x/y
 template <bool SKEW>
-__device__ __noinline__ void horner_full(const State &s, int n, uint32_t mask, const double *c, bool achro,
+UFO_DEV void horner_full(const State &s, int n, uint32_t mask, const double *c, bool achro,
                          double &pxd, double &pyd) {
   // coefficient j: its value if bit j is set, else a literal 0.
   auto coef = [&](int j) -> double {
@@ -298,14 +298,22 @@ UFO_DEV void weak(State &s, int flags, double W, bool bad) {
   }
 }
 
+
+// out-of-line kick (defined at the end of this file)
+struct PxPy { double px, py; };
+template <bool FMA>
+__device__ __noinline__ PxPy kick_ool(double x, double y, double px, double py, double o,
+                                      bool bad_o, int nn, int ns, uint32_t mn, uint32_t ms,
+                                      const double *c, bool achro, bool bad);
+
 // ---------------------------------------------------------------- teapot
 // methods.teapot (ufo/methods.py:79-97): outer drift, N-1 x (kick, weak,
 // inner drift), kick, weak, outer drift.  Table: [outer][inner][kick][W].
-template <bool FMA>
+template <bool FMA, bool FULL>
 UFO_DEV void teapot(State &s, const Op &op, const double *c) {
   const int N = op.i0, nn = op.i1, ns = op.i2;
   const uint32_t mn = static_cast<uint32_t>(op.i3), ms = static_cast<uint32_t>(op.i4);
-  const bool exact = op.flags & F_EXACT, achro = op.flags & F_ACHRO;
+  const bool exact = FULL && (op.flags & F_EXACT), achro = op.flags & F_ACHRO;
   const int fo = (op.flags >> SH_FOUTER) & 3, fi = (op.flags >> SH_FINNER) & 3;
   const double *co = c;
   const double *ci = co + drift_nconst(fo, exact);
@@ -327,7 +335,10 @@ UFO_DEV void teapot(State &s, const Op &op, const double *c) {
   for (int sl = 0; sl < N; ++sl) {
     const bool bad = s.bad_o || nf(s.x) || nf(s.y);
     if (bad || pat == 0) {
-      kick<FMA>(s, nn, ns, mn, ms, ck, achro, bad);
+      const PxPy r = kick_ool<FMA>(s.x, s.y, s.px, s.py, s.o, s.bad_o, nn, ns, mn, ms, ck, achro,
+                                   bad);
+      s.px = r.px;
+      s.py = r.py;
     } else if (pat == 1) {
       if (FMA) {
         s.px = fma_(-t, s.x, s.px);
@@ -357,13 +368,14 @@ UFO_DEV void teapot(State &s, const Op &op, const double *c) {
 //   curvature = A (* o);  psi = e - 2*curv*fringe/cos(e)*(1 + sin(e)^2)
 //   px += x*curv*tan(e);  py -= y*curv*tan(psi)
 // table: [A, T1, T2] or, per-particle psi, [A, T1, e, fringe, cos e, 1+sin^2 e]
+template <bool FULL>
 UFO_DEV void edge(State &s, int flags, const double *c) {
   const bool achro = flags & F_ACHRO;
   // both terms structurally zero (e = psi = 0): only NaN/inf can propagate
   if (!(flags & (F_T1 | F_T2)) && !(s.bad_o || nf(s.x) || nf(s.y))) return;
   const double curv = achro ? ld(c) : mul(ld(c), s.o);
   double t2;
-  if (flags & F_RTPSI) {
+  if (FULL && (flags & F_RTPSI)) {
     const double psi = sub(ld(c + 2), mul(dvd(mul(mul(2.0, curv), ld(c + 3)), ld(c + 4)),
                                           ld(c + 5)));
     t2 = tan(psi);
@@ -395,7 +407,7 @@ UFO_DEV Trig trig(double k2l) {
 
 // methods.quadrupole thick branch (ufo/methods.py:103-134);
 // table [k, L*f, (k2, C, S, CH, SH)]
-__device__ __noinline__ void thick_quad(State &s, int flags, const double *c) {
+UFO_DEV void thick_quad(State &s, int flags, const double *c) {
   const double k = ld(c), Lf = ld(c + 1);
   double k2;
   Trig t;
@@ -422,7 +434,7 @@ __device__ __noinline__ void thick_quad(State &s, int flags, const double *c) {
 
 // methods.sbend thick branch (ufo/methods.py:140-196); table
 // [A/L, k1, L*f, (kv, k2v, Cv, Sv, CHv, SHv, kx, k2x, Cx, Sx, CHx, SHx, |kx|)]
-__device__ __noinline__ void thick_bend(State &s, int flags, const double *c) {
+UFO_DEV void thick_bend(State &s, int flags, const double *c) {
   const bool achro = flags & F_ACHRO;
   const double Lf = ld(c + 2);
   const double curv = achro ? ld(c) : mul(ld(c), s.o);
@@ -474,7 +486,7 @@ __device__ __noinline__ void thick_bend(State &s, int flags, const double *c) {
 
 // ---------------------------------------------------------------- wire
 // methods.wire (ufo/methods.py:230-241); table [xw, yw, k]
-__device__ __noinline__ void wire(State &s, const double *c) {
+UFO_DEV void wire(State &s, const double *c) {
   const double wx = ld(c), wy = ld(c + 1), wk = ld(c + 2);
   const double alpha = atan2(sub(wy, s.y), sub(wx, s.x));
   const double B = dvd(wk, hypot(sub(wx, s.x), sub(wy, s.y)));
@@ -487,7 +499,7 @@ __device__ __noinline__ void wire(State &s, const double *c) {
 // ---------------------------------------------------------------- aperture
 // stack program of ``{window} == 0`` (ufo_gb300/aperture.py); table holds
 // (opcode, value) pairs.  Returns true when the particle is lost.
-__device__ __noinline__ bool aperture_lost(const State &s, const double *c, int n) {
+UFO_DEV bool aperture_lost(const State &s, const double *c, int n) {
   double st[16];
   int sp = 0;
   for (int i = 0; i < n; ++i) {
@@ -535,6 +547,65 @@ __device__ __noinline__ bool aperture_lost(const State &s, const double *c, int 
 UFO_DEV void align(State &s, int flags, const double *c) {
   if (flags & F_AX) s.x = sub(s.x, ld(c));
   if (flags & F_AY) s.y = sub(s.y, ld(c + 1));
+}
+
+}  // namespace ufo
+
+namespace ufo {
+
+// ------------------------------------------------------- out-of-line paths
+// Rare or heavy ops run out of line with by-value arguments, so the caller's
+// particle state stays in registers and the hot interpreter loop keeps a
+// small register footprint (the FP64 pipe is per SM: all of a launch's warps
+// must be resident at once).
+struct P4 { double x, px, y, py; };
+
+template <bool FMA>
+__device__ __noinline__ PxPy kick_ool(double x, double y, double px, double py, double o,
+                                      bool bad_o, int nn, int ns, uint32_t mn, uint32_t ms,
+                                      const double *c, bool achro, bool bad) {
+  State s{};
+  s.x = x; s.y = y; s.px = px; s.py = py; s.o = o; s.bad_o = bad_o;
+  kick<FMA>(s, nn, ns, mn, ms, c, achro, bad);
+  return {s.px, s.py};
+}
+
+__device__ __noinline__ P4 thick_quad_ool(double x, double px, double y, double py, double o,
+                                          int flags, const double *c) {
+  State s{};
+  s.x = x; s.px = px; s.y = y; s.py = py; s.o = o;
+  thick_quad(s, flags, c);
+  return {s.x, s.px, s.y, s.py};
+}
+
+__device__ __noinline__ P4 thick_bend_ool(double x, double px, double y, double py, double dp,
+                                          double o, int flags, const double *c) {
+  State s{};
+  s.x = x; s.px = px; s.y = y; s.py = py; s.dp = dp; s.o = o;
+  thick_bend(s, flags, c);
+  return {s.x, s.px, s.y, s.py};
+}
+
+__device__ __noinline__ P4 wire_ool(double x, double px, double y, double py, const double *c) {
+  State s{};
+  s.x = x; s.px = px; s.y = y; s.py = py;
+  wire(s, c);
+  return {s.x, s.px, s.y, s.py};
+}
+
+__device__ __noinline__ bool aperture_ool(double x, double px, double y, double py, double z,
+                                          double dp, double o, int turn, const double *c, int n) {
+  State s{};
+  s.x = x; s.px = px; s.y = y; s.py = py; s.z = z; s.dp = dp; s.o = o; s.turn = turn;
+  return aperture_lost(s, c, n);
+}
+
+__device__ __noinline__ PxPy edge_ool(double x, double y, double px, double py, double o,
+                                      bool bad_o, int flags, const double *c) {
+  State s{};
+  s.x = x; s.y = y; s.px = px; s.py = py; s.o = o; s.bad_o = bad_o;
+  edge<true>(s, flags, c);
+  return {s.px, s.py};
 }
 
 }  // namespace ufo

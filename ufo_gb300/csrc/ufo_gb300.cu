@@ -81,7 +81,10 @@ UFO_DEV void observe(const State &s, const TrackArgs &a, int64_t p, int k) {
 }
 
 // one pass through the line
-template <bool FMA>
+// FULL = false: the lean interpreter for programs made only of drifts, teapot
+// elements, kicks, alignments, constant edges, circular apertures and
+// observation points (chosen on the host); it carries far fewer live values.
+template <bool FMA, bool FULL>
 UFO_DEV void one_turn(State &s, const TrackArgs &a, const double *tab, int64_t p) {
   for (int i = 0; i < a.n_ops; ++i) {
     const int4 w0 = __ldg(reinterpret_cast<const int4 *>(a.ops + i));
@@ -90,38 +93,56 @@ UFO_DEV void one_turn(State &s, const TrackArgs &a, const double *tab, int64_t p
     const double *c = tab + op.toff;
     switch (op.kind) {
       case OP_TEAPOT:
-        teapot<FMA>(s, op, c);
+        teapot<FMA, FULL>(s, op, c);
         break;
       case OP_DRIFT:
-        drift<FMA>(s, op.i0, op.flags & F_EXACT, c);
+        drift<FMA>(s, op.i0, FULL && (op.flags & F_EXACT), c);
         break;
       case OP_KICK: {
         const bool bad = s.bad_o || nf(s.x) || nf(s.y);
-        kick<FMA>(s, op.i0, op.i1, static_cast<uint32_t>(op.i2), static_cast<uint32_t>(op.i3), c,
-                  op.flags & F_ACHRO, bad);
+        const PxPy r = kick_ool<FMA>(s.x, s.y, s.px, s.py, s.o, s.bad_o, op.i0, op.i1,
+                                     static_cast<uint32_t>(op.i2), static_cast<uint32_t>(op.i3),
+                                     c, op.flags & F_ACHRO, bad);
+        s.px = r.px;
+        s.py = r.py;
         break;
       }
       case OP_ALIGN:
         align(s, op.flags, c);
         break;
       case OP_EDGE:
-        edge(s, op.flags, c);
+        if (FULL && (op.flags & F_RTPSI)) {
+          const PxPy r = edge_ool(s.x, s.y, s.px, s.py, s.o, s.bad_o, op.flags, c);
+          s.px = r.px;
+          s.py = r.py;
+        } else {
+          edge<false>(s, op.flags, c);
+        }
         break;
       case OP_THICKQ:
-        thick_quad(s, op.flags, c);
+        if (FULL) {
+          const P4 r = thick_quad_ool(s.x, s.px, s.y, s.py, s.o, op.flags, c);
+          s.x = r.x; s.px = r.px; s.y = r.y; s.py = r.py;
+        }
         break;
       case OP_THICKB:
-        thick_bend(s, op.flags, c);
+        if (FULL) {
+          const P4 r = thick_bend_ool(s.x, s.px, s.y, s.py, s.dp, s.o, op.flags, c);
+          s.x = r.x; s.px = r.px; s.y = r.y; s.py = r.py;
+        }
         break;
       case OP_WIRE:
-        wire(s, c);
+        if (FULL) {
+          const P4 r = wire_ool(s.x, s.px, s.y, s.py, c);
+          s.x = r.x; s.px = r.px; s.y = r.y; s.py = r.py;
+        }
         break;
       case OP_APERTURE: {
         bool lost;
-        if (op.flags & F_CIRCLE)  // (x*x + y*y < c) == 0
+        if (!FULL || (op.flags & F_CIRCLE))  // (x*x + y*y < c) == 0
           lost = !(add(mul(s.x, s.x), mul(s.y, s.y)) < ld(c));
         else
-          lost = aperture_lost(s, c, op.i0);
+          lost = aperture_ool(s.x, s.px, s.y, s.py, s.z, s.dp, s.o, s.turn, c, op.i0);
         if (lost) s.x = __longlong_as_double(0x7ff8000000000000ll);
         break;
       }
@@ -139,9 +160,9 @@ UFO_DEV bool is_lost(const State &s, int mode) {
   return fabs(s.x) > 1. || fabs(s.y) > 1. || isnan(s.x);
 }
 
-template <bool FMA>
+template <bool FMA, bool FULL>
 __global__ void __launch_bounds__(32) track_kernel(TrackArgs a) {
-  const unsigned FULL = 0xffffffffu;
+  const unsigned ALL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const unsigned lt_mask = (1u << lane) - 1u;
   int64_t p = -1;
@@ -151,12 +172,12 @@ __global__ void __launch_bounds__(32) track_kernel(TrackArgs a) {
   const double *tab = a.table;
   while (true) {
     // lanes without a particle take the next ones from the queue
-    const unsigned need = __ballot_sync(FULL, p < 0 && !exhausted);
+    const unsigned need = __ballot_sync(ALL, p < 0 && !exhausted);
     if (need) {
       const int leader = __ffs(need) - 1;
       unsigned long long base = 0;
       if (lane == leader) base = atomicAdd(a.queue, static_cast<unsigned long long>(__popc(need)));
-      base = __shfl_sync(FULL, base, leader);
+      base = __shfl_sync(ALL, base, leader);
       if (p < 0 && !exhausted) {
         const int64_t q = static_cast<int64_t>(base) + __popc(need & lt_mask);
         if (q < a.n) {
@@ -174,9 +195,9 @@ __global__ void __launch_bounds__(32) track_kernel(TrackArgs a) {
       }
       continue;  // re-check: a lane that got a zero-turn particle needs another
     }
-    if (__all_sync(FULL, p < 0)) break;
+    if (__all_sync(ALL, p < 0)) break;
     if (p >= 0) {
-      one_turn<FMA>(s, a, tab, p);
+      one_turn<FMA, FULL>(s, a, tab, p);
       const bool lost = is_lost(s, a.mode);
       if (!lost) ++s.turn;
       if (lost || s.turn >= target) {
@@ -189,7 +210,7 @@ __global__ void __launch_bounds__(32) track_kernel(TrackArgs a) {
 
 // plain variant: one thread per particle, no refill (the reference's
 // one-work-item-per-particle launch shape, used for comparisons)
-template <bool FMA>
+template <bool FMA, bool FULL>
 __global__ void __launch_bounds__(128) track_plain_kernel(TrackArgs a) {
   const int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
   if (p >= a.n) return;
@@ -198,7 +219,7 @@ __global__ void __launch_bounds__(128) track_plain_kernel(TrackArgs a) {
   const int target = a.pturns ? a.pturns[p] : a.turns;
   const double *tab = a.table + (a.seed ? static_cast<int64_t>(a.seed[p]) : 0) * a.stride;
   while (s.turn < target) {
-    one_turn<FMA>(s, a, tab, p);
+    one_turn<FMA, FULL>(s, a, tab, p);
     if (is_lost(s, a.mode)) break;
     ++s.turn;
   }
@@ -241,6 +262,7 @@ struct ufo_prog {
   int64_t stride;
   int n_seeds;
   int n_dumps;
+  bool full;  // needs the full interpreter (thick, wire, exact, ...)
 };
 
 namespace {
@@ -358,6 +380,19 @@ bool aperture_ok(const double *prog, int n) {
   return n == 0 || sp >= 1;
 }
 
+// ops the lean interpreter does not carry
+bool needs_full(const int32_t *ops, int n_ops) {
+  for (int i = 0; i < n_ops; ++i) {
+    const int32_t *w = ops + i * UFO_OP_WORDS;
+    const int kind = w[0], flags = w[1];
+    if (kind == ufo::OP_THICKQ || kind == ufo::OP_THICKB || kind == ufo::OP_WIRE) return true;
+    if ((kind == ufo::OP_DRIFT || kind == ufo::OP_TEAPOT) && (flags & ufo::F_EXACT)) return true;
+    if (kind == ufo::OP_EDGE && (flags & ufo::F_RTPSI)) return true;
+    if (kind == ufo::OP_APERTURE && !(flags & ufo::F_CIRCLE)) return true;
+  }
+  return false;
+}
+
 int validate_ops(const int32_t *ops, int n_ops, int64_t stride, const double *table) {
   for (int i = 0; i < n_ops; ++i) {
     const int32_t *w = ops + i * UFO_OP_WORDS;
@@ -400,23 +435,29 @@ int launch_track(ufo_ctx *ctx, const ufo_prog *prog, const double *d_coords, con
   a.final_state = d_final;
   a.queue = ctx->queue;
   const bool fma = flags & UFO_TRACK_FMA;
+  const bool full = prog->full;
   if (flags & UFO_TRACK_PLAIN) {
-    const int64_t blocks = (n + 127) / 128;
+    const unsigned blocks = static_cast<unsigned>((n + 127) / 128);
     if (fma)
-      ufo::track_plain_kernel<true><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(a);
+      full ? ufo::track_plain_kernel<true, true><<<blocks, 128, 0, stream>>>(a)
+           : ufo::track_plain_kernel<true, false><<<blocks, 128, 0, stream>>>(a);
     else
-      ufo::track_plain_kernel<false><<<static_cast<unsigned>(blocks), 128, 0, stream>>>(a);
+      full ? ufo::track_plain_kernel<false, true><<<blocks, 128, 0, stream>>>(a)
+           : ufo::track_plain_kernel<false, false><<<blocks, 128, 0, stream>>>(a);
   } else {
     UFO_CUDA(cudaMemsetAsync(ctx->queue, 0, sizeof(unsigned long long), stream));
     // one warp per block so the block scheduler spreads warps evenly over the
-    // SMs (the FP64 pipe is per SM); at most 16 resident warps per SM
+    // SMs (the FP64 pipe is per SM); at most warps_per_sm resident per SM
     int64_t warps = (n + 31) / 32;
     const int64_t max_warps = static_cast<int64_t>(ctx->sm_count) * ctx->warps_per_sm;
     if (warps > max_warps) warps = max_warps;
+    const unsigned g = static_cast<unsigned>(warps);
     if (fma)
-      ufo::track_kernel<true><<<static_cast<unsigned>(warps), 32, 0, stream>>>(a);
+      full ? ufo::track_kernel<true, true><<<g, 32, 0, stream>>>(a)
+           : ufo::track_kernel<true, false><<<g, 32, 0, stream>>>(a);
     else
-      ufo::track_kernel<false><<<static_cast<unsigned>(warps), 32, 0, stream>>>(a);
+      full ? ufo::track_kernel<false, true><<<g, 32, 0, stream>>>(a)
+           : ufo::track_kernel<false, false><<<g, 32, 0, stream>>>(a);
   }
   ctx->launches.fetch_add(1);
   UFO_CUDA(cudaGetLastError());
@@ -537,6 +578,7 @@ int ufo_prog_create(ufo_ctx *ctx, const int32_t *ops, int n_ops, const double *t
   p->stride = stride;
   p->n_seeds = n_seeds;
   p->n_dumps = n_dumps;
+  p->full = needs_full(ops, n_ops);
   p->ops = nullptr;
   p->table = nullptr;
   const size_t ob = sizeof(ufo::Op) * (n_ops > 0 ? n_ops : 1);
