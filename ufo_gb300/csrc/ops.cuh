@@ -48,9 +48,11 @@ UFO_DEV bool nf(double v) { return (__double2hiint(v) & 0x7ff00000) == 0x7ff0000
 // exact under FMA) returns RN(a/d) (P. Markstein, IBM J. Res. Dev. 34 (1990);
 // Muller et al., Handbook of Floating-Point Arithmetic, ch. 4).  Operands far
 // from the unit range, zeros and non-finite values take IEEE division.
+__device__ __noinline__ double div_ieee(double a, double d) { return __ddiv_rn(a, d); }
+
 UFO_DEV double divc(double a, double d, double r) {
   const unsigned e = static_cast<unsigned>(__double2hiint(a)) & 0x7ff00000u;
-  if (e < 0x07700000u || e > 0x77f00000u) return dvd(a, d);
+  if (e < 0x07700000u || e > 0x77f00000u) return div_ieee(a, d);
   const double q0 = mul(a, r);
   const double rem = fma_(-q0, d, a);
   return fma_(rem, r, q0);
@@ -301,6 +303,7 @@ UFO_DEV void weak(State &s, int flags, double W, bool bad) {
 
 // out-of-line kick (defined at the end of this file)
 struct PxPy { double px, py; };
+struct P4 { double x, px, y, py; };
 template <bool FMA>
 __device__ __noinline__ PxPy kick_ool(double x, double y, double px, double py, double o,
                                       bool bad_o, int nn, int ns, uint32_t mn, uint32_t ms,
@@ -309,58 +312,153 @@ __device__ __noinline__ PxPy kick_ool(double x, double y, double px, double py, 
 // ---------------------------------------------------------------- teapot
 // methods.teapot (ufo/methods.py:79-97): outer drift, N-1 x (kick, weak,
 // inner drift), kick, weak, outer drift.  Table: [outer][inner][kick][W].
-template <bool FMA, bool FULL>
-UFO_DEV void teapot(State &s, const Op &op, const double *c) {
+//
+// The FP64 pipe of this GPU charges a predicated-off instruction like an
+// executed one, so no runtime `if` may guard FP64 arithmetic in the hot path:
+// every variant (kick pattern x inner-drift form x weak term) is its own
+// instantiation reached through a switch, and the rare paths (non-finite
+// coordinates, general multipoles) are out-of-line calls.
+//
+// Kick pattern.  The reference recomputes (K*oodppo) in every slice; it is
+// the same value each time, so it is formed once per element.
+//   1: quadrupole  px -= t*x, py += t*y            t = K*o
+//   2: sextupole   a = t*x, b = t*y; px -= a*x - b*y; py += a*y + b*x,
+//                  t = (K*o)*0.5 (scaling by 0.5 commutes with rounding)
+//   3: no kick terms (bend without gradient)
+//   0: general Horner (out of line)
+// Achromatic coefficients are multiplied by 1.0 instead of o (exact), so the
+// choice needs no branch.
+
+template <bool FMA>
+UFO_DEV void drift_L(State &s, double L) {
+  if (FMA) {
+    s.x = fma_(s.px, L, s.x);
+    s.y = fma_(s.py, L, s.y);
+  } else {
+    s.x = add(s.x, mul(s.px, L));
+    s.y = add(s.y, mul(s.py, L));
+  }
+}
+
+// x += px * (A) / d  ==  x + ((px*A)/d); FMA mode: x + px*(A/d)
+template <bool FMA>
+UFO_DEV void drift_div(State &s, const double *c) {
+  if (FMA) {
+    const double aod = ld(c + 3);
+    s.x = fma_(s.px, aod, s.x);
+    s.y = fma_(s.py, aod, s.y);
+  } else {
+    const double A = ld(c), d = ld(c + 1), r = ld(c + 2);
+    s.x = add(s.x, divc(mul(s.px, A), d, r));
+    s.y = add(s.y, divc(mul(s.py, A), d, r));
+  }
+}
+
+// one slice with the untrimmed (reference) expressions: non-finite x or y
+template <bool FMA>
+__device__ __noinline__ PxPy slow_slice(double x, double y, double px, double py, double o,
+                                        bool bad_o, int nn, int ns, uint32_t mn, uint32_t ms,
+                                        const double *ck, bool achro, bool has_weak, double W);
+
+template <bool FMA, int PAT, bool WEAK>
+UFO_DEV void tp_slice(State &s, int nn, int ns, uint32_t mn, uint32_t ms, const double *ck,
+                      bool achro, double t, double W) {
+  if (s.bad_o || nf(s.x) || nf(s.y)) {
+    const PxPy r = slow_slice<FMA>(s.x, s.y, s.px, s.py, s.o, s.bad_o, nn, ns, mn, ms, ck, achro,
+                                   WEAK, W);
+    s.px = r.px;
+    s.py = r.py;
+    return;
+  }
+  if (PAT == 0) {
+    const PxPy r = kick_ool<FMA>(s.x, s.y, s.px, s.py, s.o, s.bad_o, nn, ns, mn, ms, ck, achro,
+                                 false);
+    s.px = r.px;
+    s.py = r.py;
+  } else if (PAT == 1) {
+    if (FMA) {
+      s.px = fma_(-t, s.x, s.px);
+      s.py = fma_(t, s.y, s.py);
+    } else {
+      s.px = sub(s.px, mul(t, s.x));
+      s.py = add(s.py, mul(t, s.y));
+    }
+  } else if (PAT == 2) {
+    const double a = mul(t, s.x), b = mul(t, s.y);
+    if (FMA) {
+      s.px = fma_(b, s.y, fma_(-a, s.x, s.px));
+      s.py = fma_(b, s.x, fma_(a, s.y, s.py));
+    } else {
+      s.px = sub(s.px, sub(mul(a, s.x), mul(b, s.y)));
+      s.py = add(s.py, add(mul(a, s.y), mul(b, s.x)));
+    }
+  }
+  if (WEAK) s.px = FMA ? fma_(-s.x, W, s.px) : sub(s.px, mul(s.x, W));
+}
+
+template <bool FMA, int PAT, bool DIVIN, bool WEAK>
+UFO_DEV void teapot_v(State &s, const Op &op, const double *c) {
   const int N = op.i0, nn = op.i1, ns = op.i2;
   const uint32_t mn = static_cast<uint32_t>(op.i3), ms = static_cast<uint32_t>(op.i4);
-  const bool exact = FULL && (op.flags & F_EXACT), achro = op.flags & F_ACHRO;
-  const int fo = (op.flags >> SH_FOUTER) & 3, fi = (op.flags >> SH_FINNER) & 3;
-  const double *co = c;
-  const double *ci = co + drift_nconst(fo, exact);
-  const double *ck = ci + (N > 1 ? drift_nconst(fi, exact) : 0);
-  const double W = (op.flags & F_WEAK) ? ld(ck + __popc(mn) + __popc(ms)) : 0.0;
-  // Kick pattern.  The reference recomputes (K*oodppo) in every slice; the
-  // value is the same each time, so it is formed once per element.
-  //   1: quadrupole  px -= t*x, py += t*y            t = K*o
-  //   2: sextupole   a = t*x, b = t*y; px -= a*x - b*y; py += a*y + b*x,
-  //                  t = (K*o)*0.5 == ((K*o)*x)/2 / x exactly
-  //   3: no kick terms (bend without gradient): only NaN/inf propagate
-  //   0: general Horner
+  const bool achro = op.flags & F_ACHRO;
+  const double Lo = ld(c);
+  const double *ci = c + 1;
+  const double *ck = ci + (N > 1 ? (DIVIN ? 4 : 1) : 0);
+  const double W = WEAK ? ld(ck + __popc(mn) + __popc(ms)) : 0.0;
+  const double o1 = achro ? 1.0 : s.o;
+  double t = 0.0;
+  if (PAT == 1) t = mul(ld(ck), o1);
+  if (PAT == 2) t = mul(mul(ld(ck), o1), 0.5);
+  const double Li = DIVIN ? 0.0 : ld(ci);
+  drift_L<FMA>(s, Lo);
+  for (int sl = 1; sl < N; ++sl) {
+    tp_slice<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, t, W);
+    if (DIVIN)
+      drift_div<FMA>(s, ci);
+    else
+      drift_L<FMA>(s, Li);
+  }
+  tp_slice<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, t, W);
+  drift_L<FMA>(s, Lo);
+}
+
+// exact-Hamiltonian teapot (rare): generic, out of line
+template <bool FMA>
+__device__ __noinline__ P4 teapot_exact_ool(double x, double px, double y, double py,
+                                            double opdp, double o, bool bad_o, Op op,
+                                            const double *c);
+
+template <bool FMA, bool FULL>
+UFO_DEV void teapot(State &s, const Op &op, const double *c) {
+  if (FULL && (op.flags & F_EXACT)) {
+    const P4 r = teapot_exact_ool<FMA>(s.x, s.px, s.y, s.py, s.opdp, s.o, s.bad_o, op, c);
+    s.x = r.x; s.px = r.px; s.y = r.y; s.py = r.py;
+    return;
+  }
+  const int nn = op.i1, ns = op.i2;
+  const uint32_t mn = static_cast<uint32_t>(op.i3);
   const int pat = ns != 0 ? 0 : (nn == 2 && mn == 2u) ? 1 : (nn == 3 && mn == 4u) ? 2
                  : mn == 0u ? 3 : 0;
-  double t = 0.0;
-  if (pat == 1) t = achro ? ld(ck) : mul(ld(ck), s.o);
-  if (pat == 2) t = mul(achro ? ld(ck) : mul(ld(ck), s.o), 0.5);
-  drift<FMA>(s, fo, exact, co);
-  for (int sl = 0; sl < N; ++sl) {
-    const bool bad = s.bad_o || nf(s.x) || nf(s.y);
-    if (bad || pat == 0) {
-      const PxPy r = kick_ool<FMA>(s.x, s.y, s.px, s.py, s.o, s.bad_o, nn, ns, mn, ms, ck, achro,
-                                   bad);
-      s.px = r.px;
-      s.py = r.py;
-    } else if (pat == 1) {
-      if (FMA) {
-        s.px = fma_(-t, s.x, s.px);
-        s.py = fma_(t, s.y, s.py);
-      } else {
-        s.px = sub(s.px, mul(t, s.x));
-        s.py = add(s.py, mul(t, s.y));
-      }
-    } else if (pat == 2) {
-      const double a = mul(t, s.x), b = mul(t, s.y);
-      if (FMA) {
-        s.px = fma_(b, s.y, fma_(-a, s.x, s.px));
-        s.py = fma_(b, s.x, fma_(a, s.y, s.py));
-      } else {
-        s.px = sub(s.px, sub(mul(a, s.x), mul(b, s.y)));
-        s.py = add(s.py, add(mul(a, s.y), mul(b, s.x)));
-      }
-    }
-    weak<FMA>(s, op.flags, W, bad);
-    if (sl < N - 1) drift<FMA>(s, fi, exact, ci);
+  const int fi = (op.flags >> SH_FINNER) & 3;
+  const int v = pat | (fi == DF_DIV ? 4 : 0) | ((op.flags & F_WEAK) ? 8 : 0);
+  switch (v) {
+    case 0: teapot_v<FMA, 0, false, false>(s, op, c); break;
+    case 1: teapot_v<FMA, 1, false, false>(s, op, c); break;
+    case 2: teapot_v<FMA, 2, false, false>(s, op, c); break;
+    case 3: teapot_v<FMA, 3, false, false>(s, op, c); break;
+    case 4: teapot_v<FMA, 0, true, false>(s, op, c); break;
+    case 5: teapot_v<FMA, 1, true, false>(s, op, c); break;
+    case 6: teapot_v<FMA, 2, true, false>(s, op, c); break;
+    case 7: teapot_v<FMA, 3, true, false>(s, op, c); break;
+    case 8: teapot_v<FMA, 0, false, true>(s, op, c); break;
+    case 9: teapot_v<FMA, 1, false, true>(s, op, c); break;
+    case 10: teapot_v<FMA, 2, false, true>(s, op, c); break;
+    case 11: teapot_v<FMA, 3, false, true>(s, op, c); break;
+    case 12: teapot_v<FMA, 0, true, true>(s, op, c); break;
+    case 13: teapot_v<FMA, 1, true, true>(s, op, c); break;
+    case 14: teapot_v<FMA, 2, true, true>(s, op, c); break;
+    default: teapot_v<FMA, 3, true, true>(s, op, c); break;
   }
-  drift<FMA>(s, fo, exact, co);
 }
 
 // ---------------------------------------------------------------- edge
@@ -368,10 +466,10 @@ UFO_DEV void teapot(State &s, const Op &op, const double *c) {
 //   curvature = A (* o);  psi = e - 2*curv*fringe/cos(e)*(1 + sin(e)^2)
 //   px += x*curv*tan(e);  py -= y*curv*tan(psi)
 // table: [A, T1, T2] or, per-particle psi, [A, T1, e, fringe, cos e, 1+sin^2 e]
+// Generic form (all flags at run time): used out of line for the rare cases.
 template <bool FULL>
 UFO_DEV void edge(State &s, int flags, const double *c) {
   const bool achro = flags & F_ACHRO;
-  // both terms structurally zero (e = psi = 0): only NaN/inf can propagate
   if (!(flags & (F_T1 | F_T2)) && !(s.bad_o || nf(s.x) || nf(s.y))) return;
   const double curv = achro ? ld(c) : mul(ld(c), s.o);
   double t2;
@@ -392,6 +490,49 @@ UFO_DEV void edge(State &s, int flags, const double *c) {
     s.py = sub(s.py, mul(mul(y0, curv), t2));
   else if (bad)
     s.py = sub(s.py, mul(mul(y0, curv), 0.0));
+}
+
+__device__ __noinline__ PxPy edge_ool(double x, double y, double px, double py, double o,
+                                      bool bad_o, int flags, const double *c);
+
+// hot-path edge with a constant tan(psi): T1/T2 presence known per variant
+template <bool FMA, bool T1, bool T2>
+UFO_DEV void edge_v(State &s, int flags, const double *c) {
+  const bool achro = flags & F_ACHRO;
+  if (!T1 && !T2) {
+    if (s.bad_o || nf(s.x) || nf(s.y)) {
+      const PxPy r = edge_ool(s.x, s.y, s.px, s.py, s.o, s.bad_o, flags, c);
+      s.px = r.px;
+      s.py = r.py;
+    }
+    return;
+  }
+  const double curv = mul(ld(c), achro ? 1.0 : s.o);
+  if (nf(s.x) || nf(s.y) || nf(curv)) {
+    const PxPy r = edge_ool(s.x, s.y, s.px, s.py, s.o, s.bad_o, flags, c);
+    s.px = r.px;
+    s.py = r.py;
+    return;
+  }
+  const double x0 = s.x, y0 = s.y;
+  if (T1) s.px = FMA ? fma_(mul(x0, curv), ld(c + 1), s.px) : add(s.px, mul(mul(x0, curv), ld(c + 1)));
+  if (T2) s.py = FMA ? fma_(-mul(y0, curv), ld(c + 2), s.py) : sub(s.py, mul(mul(y0, curv), ld(c + 2)));
+}
+
+template <bool FMA, bool FULL>
+UFO_DEV void edge_dispatch(State &s, int flags, const double *c) {
+  if (FULL && (flags & F_RTPSI)) {
+    const PxPy r = edge_ool(s.x, s.y, s.px, s.py, s.o, s.bad_o, flags, c);
+    s.px = r.px;
+    s.py = r.py;
+    return;
+  }
+  switch ((flags & F_T1 ? 1 : 0) | (flags & F_T2 ? 2 : 0)) {
+    case 0: edge_v<FMA, false, false>(s, flags, c); break;
+    case 1: edge_v<FMA, true, false>(s, flags, c); break;
+    case 2: edge_v<FMA, false, true>(s, flags, c); break;
+    default: edge_v<FMA, true, true>(s, flags, c); break;
+  }
 }
 
 // ---------------------------------------------------------------- thick
@@ -558,8 +699,6 @@ namespace ufo {
 // particle state stays in registers and the hot interpreter loop keeps a
 // small register footprint (the FP64 pipe is per SM: all of a launch's warps
 // must be resident at once).
-struct P4 { double x, px, y, py; };
-
 template <bool FMA>
 __device__ __noinline__ PxPy kick_ool(double x, double y, double px, double py, double o,
                                       bool bad_o, int nn, int ns, uint32_t mn, uint32_t ms,
@@ -606,6 +745,48 @@ __device__ __noinline__ PxPy edge_ool(double x, double y, double px, double py, 
   s.x = x; s.y = y; s.px = px; s.py = py; s.o = o; s.bad_o = bad_o;
   edge<true>(s, flags, c);
   return {s.px, s.py};
+}
+
+}  // namespace ufo
+
+namespace ufo {
+
+template <bool FMA>
+__device__ __noinline__ PxPy slow_slice(double x, double y, double px, double py, double o,
+                                        bool bad_o, int nn, int ns, uint32_t mn, uint32_t ms,
+                                        const double *ck, bool achro, bool has_weak, double W) {
+  State s{};
+  s.x = x; s.y = y; s.px = px; s.py = py; s.o = o; s.bad_o = bad_o;
+  kick<FMA>(s, nn, ns, mn, ms, ck, achro, true);
+  s.px = sub(s.px, mul(s.x, has_weak ? W : 0.0));
+  return {s.px, s.py};
+}
+
+// the generic teapot with exact drifts (EXACT flag)
+template <bool FMA>
+__device__ __noinline__ P4 teapot_exact_ool(double x, double px, double y, double py,
+                                            double opdp, double o, bool bad_o, Op op,
+                                            const double *c) {
+  State s{};
+  s.x = x; s.px = px; s.y = y; s.py = py; s.opdp = opdp; s.o = o; s.bad_o = bad_o;
+  const int N = op.i0, nn = op.i1, ns = op.i2;
+  const uint32_t mn = static_cast<uint32_t>(op.i3), ms = static_cast<uint32_t>(op.i4);
+  const bool achro = op.flags & F_ACHRO;
+  const double *co = c, *ci = c + 1, *ck = ci + (N > 1 ? 1 : 0);
+  const bool has_weak = op.flags & F_WEAK;
+  const double W = has_weak ? ld(ck + __popc(mn) + __popc(ms)) : 0.0;
+  drift<FMA>(s, DF_MUL, true, co);
+  for (int sl = 0; sl < N; ++sl) {
+    const bool bad = s.bad_o || nf(s.x) || nf(s.y);
+    kick<FMA>(s, nn, ns, mn, ms, ck, achro, bad);
+    if (has_weak)
+      s.px = FMA ? fma_(-s.x, W, s.px) : sub(s.px, mul(s.x, W));
+    else if (bad)
+      s.px = sub(s.px, mul(s.x, 0.0));
+    if (sl < N - 1) drift<FMA>(s, DF_MUL, true, ci);
+  }
+  drift<FMA>(s, DF_MUL, true, co);
+  return {s.x, s.px, s.y, s.py};
 }
 
 }  // namespace ufo

@@ -96,7 +96,14 @@ UFO_DEV void one_turn(State &s, const TrackArgs &a, const double *tab, int64_t p
         teapot<FMA, FULL>(s, op, c);
         break;
       case OP_DRIFT:
-        drift<FMA>(s, op.i0, FULL && (op.flags & F_EXACT), c);
+        if (FULL && (op.flags & F_EXACT))
+          drift<FMA>(s, DF_MUL, true, c);
+        else if (op.i0 == DF_MUL)
+          drift_L<FMA>(s, ld(c));
+        else if (op.i0 == DF_DIV)
+          drift_div<FMA>(s, c);
+        else
+          drift<FMA>(s, DF_MUL2, false, c);
         break;
       case OP_KICK: {
         const bool bad = s.bad_o || nf(s.x) || nf(s.y);
@@ -108,16 +115,15 @@ UFO_DEV void one_turn(State &s, const TrackArgs &a, const double *tab, int64_t p
         break;
       }
       case OP_ALIGN:
-        align(s, op.flags, c);
+        switch ((op.flags & F_AX ? 1 : 0) | (op.flags & F_AY ? 2 : 0)) {
+          case 1: s.x = sub(s.x, ld(c)); break;
+          case 2: s.y = sub(s.y, ld(c + 1)); break;
+          case 3: s.x = sub(s.x, ld(c)); s.y = sub(s.y, ld(c + 1)); break;
+          default: break;
+        }
         break;
       case OP_EDGE:
-        if (FULL && (op.flags & F_RTPSI)) {
-          const PxPy r = edge_ool(s.x, s.y, s.px, s.py, s.o, s.bad_o, op.flags, c);
-          s.px = r.px;
-          s.py = r.py;
-        } else {
-          edge<false>(s, op.flags, c);
-        }
+        edge_dispatch<FMA, FULL>(s, op.flags, c);
         break;
       case OP_THICKQ:
         if (FULL) {
