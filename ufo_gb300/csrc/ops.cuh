@@ -646,6 +646,10 @@ UFO_DEV bool aperture_lost(const State &s, const double *c, int n) {
   for (int i = 0; i < n; ++i) {
     const int op = static_cast<int>(ld(c + 2 * i));
     const double v = ld(c + 2 * i + 1);
+    // depth guards: a malformed program stops instead of leaving the stack
+    const int need = (op == 1 || op == 2) ? 0 : (op == 3 || op == 4 || op == 19 || op == 20) ? 1
+                   : op == 21 ? 3 : 2;
+    if (sp < need || ((op == 1 || op == 2) && sp >= 16)) return false;
     if (op == 1) { st[sp++] = v; continue; }
     if (op == 2) {
       const int k = static_cast<int>(v);

@@ -190,8 +190,12 @@ __global__ void __launch_bounds__(32) track_kernel(TrackArgs a) {
           p = q;
           load_particle(s, a, p);
           target = a.pturns ? a.pturns[p] : a.turns;
-          tab = a.table + (a.seed ? static_cast<int64_t>(a.seed[p]) : 0) * a.stride;
-          if (target <= 0) {  // nothing to track
+          const int64_t sd = a.seed ? static_cast<int64_t>(a.seed[p]) : 0;
+          tab = a.table + sd * a.stride;
+          if (sd < 0 || sd >= a.n_seeds) {  // seed outside the table: not tracked
+            if (a.lost) a.lost[p] = 0xffffffffu;
+            p = -1;
+          } else if (target <= 0) {  // nothing to track
             store_final(s, a, p);
             p = -1;
           }
@@ -223,7 +227,12 @@ __global__ void __launch_bounds__(128) track_plain_kernel(TrackArgs a) {
   State s{};
   load_particle(s, a, p);
   const int target = a.pturns ? a.pturns[p] : a.turns;
-  const double *tab = a.table + (a.seed ? static_cast<int64_t>(a.seed[p]) : 0) * a.stride;
+  const int64_t sd = a.seed ? static_cast<int64_t>(a.seed[p]) : 0;
+  if (sd < 0 || sd >= a.n_seeds) {  // seed outside the table: not tracked
+    if (a.lost) a.lost[p] = 0xffffffffu;
+    return;
+  }
+  const double *tab = a.table + sd * a.stride;
   while (s.turn < target) {
     one_turn<FMA, FULL>(s, a, tab, p);
     if (is_lost(s, a.mode)) break;
@@ -409,24 +418,57 @@ int validate_ops(const int32_t *ops, int n_ops, int64_t stride, const double *ta
     if (w[2] < 0 || w[2] + nc > stride)
       return fail(UFO_E_ARG, "op %d: constants [%d, %lld) outside stride %lld", i, w[2],
                   static_cast<long long>(w[2] + nc), static_cast<long long>(stride));
-    if (w[0] == ufo::OP_APERTURE && !(w[1] & ufo::F_CIRCLE) && !aperture_ok(table + w[2], w[3]))
+    if (w[0] == ufo::OP_APERTURE && !(w[1] & ufo::F_CIRCLE) && table &&
+        !aperture_ok(table + w[2], w[3]))
       return fail(UFO_E_ARG, "op %d: malformed aperture program", i);
   }
   return UFO_OK;
 }
 
-int launch_track(ufo_ctx *ctx, const ufo_prog *prog, const double *d_coords, const int32_t *d_seed,
-                 const int32_t *d_pturns, int64_t n, int turns, int mode, int flags, int64_t slots,
-                 int every, double *d_tracks, uint32_t *d_lost, double *d_final,
-                 cudaStream_t stream) {
-  if (n <= 0) return UFO_OK;
+// The launch shared by every entry point: fill the kernel arguments and start
+// the persistent (or plain) kernel on `stream`; `queue` is the work counter.
+int launch_kernels(ufo::TrackArgs &a, bool full, int sm_count, int warps_per_sm,
+                   cudaStream_t stream) {
+  const bool fma = a.flags & UFO_TRACK_FMA;
+  if (a.flags & UFO_TRACK_PLAIN) {
+    const unsigned blocks = static_cast<unsigned>((a.n + 127) / 128);
+    if (fma)
+      full ? ufo::track_plain_kernel<true, true><<<blocks, 128, 0, stream>>>(a)
+           : ufo::track_plain_kernel<true, false><<<blocks, 128, 0, stream>>>(a);
+    else
+      full ? ufo::track_plain_kernel<false, true><<<blocks, 128, 0, stream>>>(a)
+           : ufo::track_plain_kernel<false, false><<<blocks, 128, 0, stream>>>(a);
+  } else {
+    UFO_CUDA(cudaMemsetAsync(a.queue, 0, sizeof(unsigned long long), stream));
+    // one warp per block so the block scheduler spreads warps evenly over the
+    // SMs (the FP64 pipe is per SM); at most warps_per_sm resident per SM
+    int64_t warps = (a.n + 31) / 32;
+    const int64_t max_warps = static_cast<int64_t>(sm_count) * warps_per_sm;
+    if (warps > max_warps) warps = max_warps;
+    const unsigned g = static_cast<unsigned>(warps);
+    if (fma)
+      full ? ufo::track_kernel<true, true><<<g, 32, 0, stream>>>(a)
+           : ufo::track_kernel<true, false><<<g, 32, 0, stream>>>(a);
+    else
+      full ? ufo::track_kernel<false, true><<<g, 32, 0, stream>>>(a)
+           : ufo::track_kernel<false, false><<<g, 32, 0, stream>>>(a);
+  }
+  UFO_CUDA(cudaGetLastError());
+  return UFO_OK;
+}
+
+ufo::TrackArgs make_args(const ufo::Op *ops, int n_ops, const double *table, int64_t stride,
+                         int n_seeds, int n_dumps, const double *d_coords, const int32_t *d_seed,
+                         const int32_t *d_pturns, int64_t n, int turns, int mode, int flags,
+                         int64_t slots, int every, double *d_tracks, uint32_t *d_lost,
+                         double *d_final, unsigned long long *queue) {
   ufo::TrackArgs a;
-  a.ops = prog->ops;
-  a.n_ops = prog->n_ops;
-  a.table = prog->table;
-  a.stride = prog->stride;
-  a.n_seeds = prog->n_seeds;
-  a.n_dumps = prog->n_dumps;
+  a.ops = ops;
+  a.n_ops = n_ops;
+  a.table = table;
+  a.stride = stride;
+  a.n_seeds = n_seeds;
+  a.n_dumps = n_dumps;
   a.coords = d_coords;
   a.seed = d_seed;
   a.pturns = d_pturns;
@@ -439,35 +481,21 @@ int launch_track(ufo_ctx *ctx, const ufo_prog *prog, const double *d_coords, con
   a.tracks = d_tracks;
   a.lost = d_lost;
   a.final_state = d_final;
-  a.queue = ctx->queue;
-  const bool fma = flags & UFO_TRACK_FMA;
-  const bool full = prog->full;
-  if (flags & UFO_TRACK_PLAIN) {
-    const unsigned blocks = static_cast<unsigned>((n + 127) / 128);
-    if (fma)
-      full ? ufo::track_plain_kernel<true, true><<<blocks, 128, 0, stream>>>(a)
-           : ufo::track_plain_kernel<true, false><<<blocks, 128, 0, stream>>>(a);
-    else
-      full ? ufo::track_plain_kernel<false, true><<<blocks, 128, 0, stream>>>(a)
-           : ufo::track_plain_kernel<false, false><<<blocks, 128, 0, stream>>>(a);
-  } else {
-    UFO_CUDA(cudaMemsetAsync(ctx->queue, 0, sizeof(unsigned long long), stream));
-    // one warp per block so the block scheduler spreads warps evenly over the
-    // SMs (the FP64 pipe is per SM); at most warps_per_sm resident per SM
-    int64_t warps = (n + 31) / 32;
-    const int64_t max_warps = static_cast<int64_t>(ctx->sm_count) * ctx->warps_per_sm;
-    if (warps > max_warps) warps = max_warps;
-    const unsigned g = static_cast<unsigned>(warps);
-    if (fma)
-      full ? ufo::track_kernel<true, true><<<g, 32, 0, stream>>>(a)
-           : ufo::track_kernel<true, false><<<g, 32, 0, stream>>>(a);
-    else
-      full ? ufo::track_kernel<false, true><<<g, 32, 0, stream>>>(a)
-           : ufo::track_kernel<false, false><<<g, 32, 0, stream>>>(a);
-  }
-  ctx->launches.fetch_add(1);
-  UFO_CUDA(cudaGetLastError());
-  return UFO_OK;
+  a.queue = queue;
+  return a;
+}
+
+int launch_track(ufo_ctx *ctx, const ufo_prog *prog, const double *d_coords, const int32_t *d_seed,
+                 const int32_t *d_pturns, int64_t n, int turns, int mode, int flags, int64_t slots,
+                 int every, double *d_tracks, uint32_t *d_lost, double *d_final,
+                 cudaStream_t stream) {
+  if (n <= 0) return UFO_OK;
+  ufo::TrackArgs a = make_args(prog->ops, prog->n_ops, prog->table, prog->stride, prog->n_seeds,
+                               prog->n_dumps, d_coords, d_seed, d_pturns, n, turns, mode, flags,
+                               slots, every, d_tracks, d_lost, d_final, ctx->queue);
+  const int rc = launch_kernels(a, prog->full, ctx->sm_count, ctx->warps_per_sm, stream);
+  if (rc == UFO_OK) ctx->launches.fetch_add(1);
+  return rc;
 }
 
 int check_track_args(ufo_ctx *ctx, const ufo_prog *prog, int64_t n, int turns, int mode,
