@@ -93,6 +93,36 @@ int ufo_track_device(ufo_ctx *ctx, const ufo_prog *prog, const double *d_coords,
                      int mode, int flags, int64_t slots, int every, double *d_tracks,
                      uint32_t *d_lost, double *d_final, void *stream);
 
+/* Largest opcode table ufo_track_noalloc accepts. */
+#define UFO_NOALLOC_MAX_OPS 8192
+
+/*
+ * Allocation-free tracking.  No counterpart in the reference (which always
+ * creates its own OpenCL buffers); it exists for callers that cannot call
+ * cudaMalloc -- programs whose GPU memory belongs to another allocator (a
+ * framework's memory pool or a fixed arena) or that must not allocate while
+ * running, such as an online model in an accelerator control loop, where an
+ * allocation could stall or fail mid-operation.  Needs no context or program
+ * object: pass the host opcode table (`ops`, int32[n_ops][8], at most
+ * UFO_NOALLOC_MAX_OPS rows, else UFO_E_ARG) and device pointers for the
+ * per-seed constants (`d_table`, f64[n_seeds][stride]), the coordinates and
+ * the outputs; the other arguments mean what they mean in ufo_track_device.
+ * Works on the current device and enqueues on `stream` (NULL: the legacy
+ * default stream) without synchronising.
+ * It calls no cudaMalloc, cudaFree or other allocating routine.  Its scratch
+ * (the staged opcode table and the work counter) is a static device array of
+ * 256.25 KiB that every GPU loading this library holds until exit.  Every call
+ * shares that array: calls that overlap on the GPU race (serialise them on one
+ * stream); each call clears the counter it needs.  The first call on a device
+ * sets up that device (resolves the array's address, uploads constant tables);
+ * make that first call before any stream capture.
+ */
+int ufo_track_noalloc(const int32_t *ops, int n_ops, const double *d_table, int64_t stride,
+                      int n_seeds, int n_dumps, const double *d_coords, const int32_t *d_seed,
+                      const int32_t *d_pturns, int64_t n, int turns, int mode, int flags,
+                      int64_t slots, int every, double *d_tracks, uint32_t *d_lost,
+                      double *d_final, void *stream);
+
 /* Kernel launches issued by this library since the context was created.
  * Diagnostic; no reference counterpart. */
 int ufo_launch_count(ufo_ctx *ctx, int64_t *count);

@@ -36,6 +36,9 @@ SIGNATURES = {
                          ctypes.c_int, P, P, P, P],
     'ufo_launch_count': [P, P],
     'ufo_fp64_peak': [P, P],
+    'ufo_track_noalloc': [P, ctypes.c_int, P, I64, ctypes.c_int, ctypes.c_int, P, P, P, I64,
+                          ctypes.c_int, ctypes.c_int, ctypes.c_int, I64, ctypes.c_int, P, P, P,
+                          P],
 }
 _VOID = {'ufo_ctx_destroy', 'ufo_prog_destroy'}
 

@@ -732,3 +732,89 @@ int ufo_track(ufo_ctx *ctx, const ufo_prog *prog, const double *coords, const in
 }
 
 }  // extern "C"
+
+// ============================================ allocation-free entry point
+//
+// ufo_track_noalloc serves callers that cannot call cudaMalloc: programs whose
+// device memory belongs to another allocator (a framework's memory pool or a
+// fixed arena) or that must not allocate while running, such as an online
+// model inside an accelerator control loop that may neither stall on nor fail
+// in an allocation mid-operation.  The caller owns every buffer it passes; the
+// only scratch this path needs -- the staged opcode table the kernel
+// interprets and the persistent kernel's work counter -- lives in the
+// file-scope array below, which every GPU that loads this library holds
+// (256 B + UFO_NOALLOC_MAX_OPS * 32 B = 256.25 KiB) until the process exits.
+namespace {
+
+struct NoallocScratch {
+  unsigned long long queue;        // work counter, cleared by every call
+  unsigned long long pad[31];      // keeps the table 256-byte aligned
+  ufo::Op ops[UFO_NOALLOC_MAX_OPS];
+};
+static __device__ __align__(256) NoallocScratch g_noalloc_scratch;
+
+struct NoallocDevice {
+  bool ready;
+  NoallocScratch *scratch;  // device address of g_noalloc_scratch
+  int sm_count;
+};
+NoallocDevice g_noalloc_dev[64];
+
+// Once per device, with that device current: resolve the array's device
+// address (in host code its name is only a host-side stand-in) and upload the
+// constant tables.  Runs on a device's first call.
+int noalloc_setup(int device) {
+  if (device < 0 || device >= 64) return fail(UFO_E_ARG, "device %d out of range", device);
+  NoallocDevice &d = g_noalloc_dev[device];
+  if (d.ready) return UFO_OK;
+  int rc = ensure_constants(device);
+  if (rc) return rc;
+  void *ptr = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+  int sms = 0;
+  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaDeviceGetAttribute");
+  d.scratch = static_cast<NoallocScratch *>(ptr);
+  d.sm_count = sms;
+  d.ready = true;
+  return UFO_OK;
+}
+
+}  // namespace
+
+extern "C" int ufo_track_noalloc(const int32_t *ops, int n_ops, const double *d_table,
+                                 int64_t stride, int n_seeds, int n_dumps, const double *d_coords,
+                                 const int32_t *d_seed, const int32_t *d_pturns, int64_t n,
+                                 int turns, int mode, int flags, int64_t slots, int every,
+                                 double *d_tracks, uint32_t *d_lost, double *d_final,
+                                 void *stream) {
+  if (!ops && n_ops > 0) return fail(UFO_E_ARG, "null opcode table");
+  if (n_ops < 0 || n_ops > UFO_NOALLOC_MAX_OPS)
+    return fail(UFO_E_ARG,
+                "opcode table of %d ops exceeds the allocation-free entry point's maximum of %d",
+                n_ops, UFO_NOALLOC_MAX_OPS);
+  if (!d_table || stride < 1 || n_seeds < 1 || n_dumps < 0)
+    return fail(UFO_E_ARG, "bad constant table (pointer, stride or seed count)");
+  if (n < 0 || turns < 0) return fail(UFO_E_ARG, "negative particle or turn count");
+  if (mode != UFO_MODE_TRACK && mode != UFO_MODE_SA) return fail(UFO_E_ARG, "bad mode %d", mode);
+  if (slots < 0 || every < 1) return fail(UFO_E_ARG, "bad observation slots or stride");
+  if (n > 0 && !d_coords) return fail(UFO_E_ARG, "null coordinates");
+  int rc = validate_ops(ops, n_ops, stride, nullptr);
+  if (rc) return rc;
+  int device = 0;
+  UFO_CUDA(cudaGetDevice(&device));
+  rc = noalloc_setup(device);
+  if (rc) return rc;
+  if (n == 0) return UFO_OK;
+  NoallocDevice &d = g_noalloc_dev[device];
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (n_ops > 0)
+    UFO_CUDA(cudaMemcpyAsync(d.scratch->ops, ops, sizeof(ufo::Op) * n_ops,
+                             cudaMemcpyHostToDevice, st));
+  ufo::TrackArgs a = make_args(d.scratch->ops, n_ops, d_table, stride, n_seeds, n_dumps,
+                               d_coords, d_seed, d_pturns, n, turns, mode,
+                               flags & ~UFO_TRACK_PLAIN, slots, every, d_tracks, d_lost, d_final,
+                               &d.scratch->queue);
+  return launch_kernels(a, needs_full(ops, n_ops), d.sm_count, 16, st);
+}
