@@ -45,7 +45,8 @@ def parse():
     ap.add_argument('--steps', type=int, default=10)
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
-    ap.add_argument('--mode', default='strict', choices=['strict', 'fma'])
+    ap.add_argument('--mode', default='fma', choices=['strict', 'fma'])
+    ap.add_argument('--no-alt', action='store_true', help='skip the other-mode measurement')
     ap.add_argument('--turns-per-step', type=int, default=1000)
     ap.add_argument('--particles', type=int, default=65536)
     ap.add_argument('--no-e2e', action='store_true')
@@ -191,6 +192,7 @@ def bench_ours(args):
     import torch
     import ufo_gb300 as u
     from ufo_gb300 import capi, compiler as C, workloads as W
+    from ufo_gb300.ranks import beam_seed, max_over_ranks
     world, rank, local = dist()
     if world > 1:
         import torch.distributed as tdist
@@ -198,15 +200,11 @@ def bench_ours(args):
     torch.cuda.set_device(local)
     dev = torch.device('cuda', local)
     ctx = u.context(local)
-    flags = u.KICK | (u.FMA if args.mode == 'fma' else 0)
-    tflags = capi.UFO_TRACK_FMA if args.mode == 'fma' else 0
     ring = W.c2_ring(u)
     n_elem = len(ring.flatten())
-    prog = C.compile_line(ring, flags, where=[-1])
-    dprog = capi.DeviceProgram(ctx, prog)
     n = args.particles
     T = args.turns_per_step
-    beam = W.c2_beam(n, seed=2 + rank)
+    beam = W.c2_beam(n, seed=beam_seed(rank))
     c0 = torch.from_numpy(beam).to(dev)
     bufs = [c0.clone(), torch.empty_like(c0)]
     lost = torch.empty(n, dtype=torch.int32, device=dev)
@@ -217,63 +215,71 @@ def bench_ours(args):
     torch.cuda.set_stream(stream)
     lib = capi.load()
 
-    def step(i, ev=None):
-        src, dst = bufs[i % 2], bufs[(i + 1) % 2]
-        if ev:
-            ev[0].record(stream)
-        capi.check(lib.ufo_track_device(ctx.handle, dprog.handle, capi.ptr(src.data_ptr()), None,
-                                        None, n, T, capi.UFO_MODE_TRACK, tflags, 0, 1, None,
-                                        capi.ptr(lost.data_ptr()), capi.ptr(dst.data_ptr()),
-                                        capi.ptr(stream.cuda_stream)))
-        if ev:
-            ev[1].record(stream)
-
     def barrier():
         torch.cuda.synchronize(dev)
         if world > 1:
             import torch.distributed as tdist
             tdist.barrier()
 
-    for i in range(args.warmup):
-        flush.zero_()
-        step(i)
-    bufs[0].copy_(c0)
-    barrier()
+    def timed_device(mode, steps, warmup):
+        """Exactly `steps` chained launches (1000 turns each) on HBM-resident
+        coordinates, L2 flushed between launches; CUDA events on the stream."""
+        flags = u.KICK | (u.FMA if mode == 'fma' else 0)
+        tflags = capi.UFO_TRACK_FMA if mode == 'fma' else 0
+        prog = C.compile_line(ring, flags, where=[-1])
+        dprog = capi.DeviceProgram(ctx, prog)
+
+        def step(i, ev=None):
+            src, dst = bufs[i % 2], bufs[(i + 1) % 2]
+            if ev:
+                ev[0].record(stream)
+            capi.check(lib.ufo_track_device(ctx.handle, dprog.handle, capi.ptr(src.data_ptr()),
+                                            None, None, n, T, capi.UFO_MODE_TRACK, tflags, 0, 1,
+                                            None, capi.ptr(lost.data_ptr()),
+                                            capi.ptr(dst.data_ptr()),
+                                            capi.ptr(stream.cuda_stream)))
+            if ev:
+                ev[1].record(stream)
+
+        for i in range(warmup):
+            flush.zero_()
+            step(i)
+        bufs[0].copy_(c0)
+        barrier()
+        l0 = ctx.launches()
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(steps)]
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for i in range(steps):
+            flush.zero_()
+            step(i, evs[i])
+        t_end.record(stream)
+        barrier()
+        total_ms = max_over_ranks(t_start.elapsed_time(t_end), dev)
+        kern_ms = [a.elapsed_time(b) for a, b in evs]
+        lost_np = lost.cpu().numpy()
+        # particle-turns tracked by the last launch (a lost particle stops)
+        pt = np.where(lost_np < T, lost_np + 1, T).astype(np.float64).sum()
+        fl = prog.flops_fast if mode == 'fma' else prog.flops
+        achieved = fl * pt / (statistics.mean(kern_ms) / 1e3) / 1e9
+        return {'value': world * n * n_elem * T * steps / (total_ms / 1e3),
+                'ms_per_step': total_ms / steps, 'kernel_ms': kern_ms,
+                'launches': ctx.launches() - l0, 'achieved': achieved,
+                'flops_per_particle_turn': fl, 'lost': int((lost_np < T).sum())}
+
     clocks = Clocks(local)
     clocks.start()
-    l0 = ctx.launches()
-    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(args.steps)]
-    t_start = torch.cuda.Event(enable_timing=True)
-    t_end = torch.cuda.Event(enable_timing=True)
-    t_start.record(stream)
-    for i in range(args.steps):
-        flush.zero_()
-        step(i, evs[i])
-    t_end.record(stream)
-    barrier()
+    main = timed_device(args.mode, args.steps, args.warmup)
     clk = clocks.stop()
-    launches = ctx.launches() - l0
-    total_ms = t_start.elapsed_time(t_end)
-    kern_ms = [a.elapsed_time(b) for a, b in evs]
-    lost_np = lost.cpu().numpy()
-    if world > 1:
-        import torch.distributed as tdist
-        t = torch.tensor([total_ms], device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * n * n_elem * T * args.steps / (total_ms / 1e3)
-    # particle-turns actually tracked in the last launch (lost particles stop)
-    pt = np.where(lost_np < T, lost_np + 1, T).astype(np.float64).sum()
-    fl = prog.flops_fast if args.mode == 'fma' else prog.flops
-    flops_launch = fl * pt
-    mean_kernel_s = statistics.mean(kern_ms) / 1e3
-    achieved = flops_launch / mean_kernel_s / 1e9
     peak = ctypes_peak(ctx)
-    traffic = load_traffic(args.mode)
+    other = 'strict' if args.mode == 'fma' else 'fma'
+    alt = None if args.no_alt else timed_device(other, min(3, args.steps), 1)
 
     e2e = None
     if not args.no_e2e:
+        flags = u.KICK | (u.FMA if args.mode == 'fma' else 0)
         tr = u.Track(ring, flags=flags | u.DOUBLE_PRECISION, turns=T, particles=n,
                      parameters=PARAMS, where=[-1], every=T, context=ctx)
         host = beam[:, [0, 1, 2, 3, 5]].copy()
@@ -288,12 +294,7 @@ def bench_ours(args):
             tr.run()
             cur = tr.final[:, [0, 1, 2, 3, 5]]
         barrier()
-        e2e_s = time.perf_counter() - t0
-        if world > 1:
-            import torch.distributed as tdist
-            t = torch.tensor([e2e_s], device=dev)
-            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-            e2e_s = float(t.item())
+        e2e_s = max_over_ranks(time.perf_counter() - t0, dev)
         e2e = {'value': world * n * n_elem * T * args.steps / e2e_s,
                'unit': 'particle*element*turns/s',
                'h2d_bytes_per_step': n * 6 * 8,
@@ -303,23 +304,31 @@ def bench_ours(args):
         return
     cb = None if args.no_cpu else cpu_baseline(n_elem)
     line = {
-        'metric': 'FP64 particle*element*turns/s', 'value': value,
+        'metric': 'FP64 particle*element*turns/s', 'value': main['value'],
         'unit': 'particle*element*turns/s', 'n_gpus': world, 'steps': args.steps,
-        'warmup': args.warmup, 'ms_per_step': total_ms / args.steps, 'higher_is_better': True,
+        'warmup': args.warmup, 'ms_per_step': main['ms_per_step'], 'higher_is_better': True,
         'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
         'config': {'workload': 'C2 light-source ring (1024 elements, teapot 4 slices, 10 mm '
                                'aperture), 65536 Gaussian particles, 10000 turns',
                    'particles_per_gpu': n, 'turns_per_step': T, 'elements': n_elem,
                    'mode': args.mode, 'l2': 'flushed (256 MiB memset) between steps',
                    'parallelism': f'weak: {n} particles per GPU, no collective'},
-        'roofline': {'bound': 'fp64', 'achieved': achieved, 'peak': peak, 'unit': 'GFLOP/s',
-                     'frac': achieved / peak if peak else None,
-                     'traffic': traffic,
-                     'flops_per_particle_turn': fl,
+        'roofline': {'bound': 'fp64', 'achieved': main['achieved'], 'peak': peak,
+                     'unit': 'GFLOP/s', 'frac': main['achieved'] / peak if peak else None,
+                     'traffic': load_traffic(args.mode),
+                     'flops_per_particle_turn': main['flops_per_particle_turn'],
                      'peak_source': 'measured live: ufo_fp64_peak (DFMA chains, 2 flop each)'},
-        'gpu_launches': launches,
-        'kernel_ms': kern_ms,
+        'gpu_launches': main['launches'],
+        'kernel_ms': main['kernel_ms'],
+        'lost_particles': main['lost'],
     }
+    if alt:
+        line[other] = {'value': alt['value'], 'ms_per_step': alt['ms_per_step'],
+                       'steps': min(3, args.steps),
+                       'roofline_frac': alt['achieved'] / peak if peak else None,
+                       'flops_per_particle_turn': alt['flops_per_particle_turn'],
+                       'note': ('bit-identical to the reference' if other == 'strict' else
+                                'fused multiply-add, within 1e-9 of strict after 1000 turns')}
     if e2e:
         line['e2e'] = e2e
     if cb:

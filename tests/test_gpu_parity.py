@@ -108,6 +108,32 @@ def test_full_size_c2_subset_vs_oracle():
     assert np.array_equal(lost[idx], ref['lost'])
 
 
+def test_full_size_c2_fma_within_tolerance_of_strict():
+    """The benchmark workload at full size: all 65,536 particles, FMA mode vs
+    the strict (reference-identical) mode: <= 1e-12 relative after 1 turn,
+    <= 1e-9 after 1000 turns, identical loss masks; strict mode itself
+    checked against the oracle on a random subset after 1000 turns."""
+    import ufo_gb300 as u
+    from ufo_gb300 import capi, compiler as C, workloads as W
+    from oracle import oracle as O
+    ring = W.c2_ring(u)
+    beam = W.c2_beam(65536)
+    ctx = u.context(0)
+    ps = capi.DeviceProgram(ctx, C.compile_line(ring, u.KICK, where=[-1]))
+    pf = capi.DeviceProgram(ctx, C.compile_line(ring, u.KICK | u.FMA, where=[-1]))
+    for turns, tol in ((1, 1e-12), (1000, 1e-9)):
+        _, ls, fs = capi.track(ctx, ps, beam, turns, capi.UFO_MODE_TRACK, 0, slots=0)
+        _, lf, ff = capi.track(ctx, pf, beam, turns, capi.UFO_MODE_TRACK, capi.UFO_TRACK_FMA,
+                               slots=0)
+        assert np.array_equal(ls, lf)
+        scale = np.max(np.abs(fs[:, :4]), axis=0)
+        err = np.max(np.abs(ff[:, :4] - fs[:, :4]) / scale)
+        assert err <= tol, (turns, err)
+    idx = np.random.default_rng(1).choice(65536, 64, replace=False)
+    ref = O.track(ring, u.KICK, beam[idx], 1000, where=[-1], tracks=False)
+    assert np.array_equal(fs[idx], ref['final'], equal_nan=True)
+
+
 def test_seed_batch_equals_individual_launches():
     """One launch over many error seeds == one launch per seed, bit for bit."""
     import ufo_gb300 as u
