@@ -51,6 +51,9 @@ def parse():
     ap.add_argument('--particles', type=int, default=65536)
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--workload', default='c2', choices=['c2', 'c4'])
+    ap.add_argument('--seeds', type=int, default=64, help='C4: number of seeds')
+    ap.add_argument('--turn-div', type=int, default=4, help='C4: divide turn counts by this')
     return ap.parse_args()
 
 
@@ -338,6 +341,65 @@ def bench_ours(args):
     print(json.dumps(line), flush=True)
 
 
+def bench_c4(args):
+    """Batched error seeds (C4): one autotuned persistent CUDA-graph launch over
+    all seeds vs one launch per seed, identical outputs required."""
+    import torch
+    import ufo_gb300 as u
+    from ufo_gb300 import workloads as W
+    torch.cuda.set_device(0)
+    ctx = u.context(0)
+    parts, turns = W.c4_sizes(512)
+    S = args.seeds
+    parts, turns = parts[:S], np.maximum(1, turns[:S] // args.turn_div)
+    ring = W.c1_ring(u)
+    params = W.c4_parameters(ring)
+    rows = W.c4_seed_rows(ring, S)
+    flags = u.KICK | (u.FMA if args.mode == 'fma' else 0)
+    b = u.TrackBatch(ring, params, rows, parts, turns, flags=flags, context=ctx)
+    b.coords[:] = W.c1_beam(b.n, seed=4)
+    tuning = u.autotune(b)
+    pet = b.particle_element_turns()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+
+    def timed(fn, reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    b.upload()
+    b.capture()
+    for _ in range(args.warmup):
+        b.launch(stream=stream.cuda_stream)
+    l0 = ctx.launches()
+    ms_batch = timed(lambda: b.launch(stream=stream.cuda_stream), args.steps)
+    launches = ctx.launches() - l0
+    fb, lb = [a.copy() for a in b.download()]
+    b.upload('seed')
+    ms_plain = timed(lambda: b.plain_launches(stream=stream.cuda_stream), 1)
+    fp, lp = b.download()
+    identical = bool(np.array_equal(fb, fp, equal_nan=True) and np.array_equal(lb, lp))
+    line = {'metric': 'FP64 particle*element*turns/s', 'value': pet / (ms_batch / 1e3),
+            'unit': 'particle*element*turns/s', 'n_gpus': 1, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': ms_batch, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+            'config': {'workload': f'C4 batched error seeds: first {S} of 512 seeds of the C1 '
+                                   f'ring with dx/dy and normal/skew errors of MAD orders 3-6, '
+                                   f'particles log-uniform 256-8192, turns U(1000, 4096) // '
+                                   f'{args.turn_div}', 'particles': b.n, 'seeds': S,
+                       'mode': args.mode, 'tuning': tuning},
+            'plain_one_launch_per_seed': {'value': pet / (ms_plain / 1e3), 'ms': ms_plain},
+            'speedup_batched_vs_plain': ms_plain / ms_batch,
+            'identical_results': identical, 'gpu_launches': launches}
+    print(json.dumps(line), flush=True)
+
+
 def ctypes_peak(ctx):
     import ctypes
     from ufo_gb300 import capi
@@ -350,6 +412,8 @@ def main():
     args = parse()
     if args.impl == 'reference':
         bench_reference(args)
+    elif args.workload == 'c4':
+        bench_c4(args)
     else:
         bench_ours(args)
 

@@ -123,6 +123,23 @@ int ufo_track_noalloc(const int32_t *ops, int n_ops, const double *d_table, int6
                       int64_t slots, int every, double *d_tracks, uint32_t *d_lost,
                       double *d_final, void *stream);
 
+/* Resident warps per SM of the persistent grid (default 16); set by the
+ * autotuner (ufo_gb300/autotune.py).  No reference counterpart. */
+int ufo_ctx_set_tuning(ufo_ctx *ctx, int warps_per_sm);
+
+/* One tracking launch (work-counter reset + persistent kernel over all
+ * particles of all seeds) captured into a CUDA graph and replayed on the same
+ * device buffers: the batched-seed path (many lattice variants with uneven
+ * particle and turn counts in one launch).  Replaces the reference's idiom of
+ * per-particle parameter rows in one NDRange (HOWTO.md:21, ufo/track.py:110). */
+typedef struct ufo_graph ufo_graph;
+int ufo_graph_create(ufo_ctx *ctx, const ufo_prog *prog, const double *d_coords,
+                     const int32_t *d_seed, const int32_t *d_pturns, int64_t n, int turns,
+                     int mode, int flags, int64_t slots, int every, double *d_tracks,
+                     uint32_t *d_lost, double *d_final, ufo_graph **out);
+int ufo_graph_launch(ufo_graph *graph, void *stream);
+void ufo_graph_destroy(ufo_graph *graph);
+
 /* Kernel launches issued by this library since the context was created.
  * Diagnostic; no reference counterpart. */
 int ufo_launch_count(ufo_ctx *ctx, int64_t *count);

@@ -23,9 +23,12 @@ def __getattr__(name):
     # the GPU drivers load the CUDA library lazily so that lattice work and the
     # CPU test-suite run without a GPU
     if name in ('Track', 'StableAperture', 'ClosedOrbit', 'Optics', 'chromaticity',
-                'list_devices', 'context', 'Context', 'TrackBatch', 'autotune'):
+                'list_devices', 'context', 'Context'):
         from . import drivers
         return getattr(drivers, name)
+    if name in ('TrackBatch', 'autotune'):
+        from . import batch
+        return getattr(batch, name)
     raise AttributeError(name)
 
 

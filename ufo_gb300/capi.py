@@ -36,11 +36,16 @@ SIGNATURES = {
                          ctypes.c_int, P, P, P, P],
     'ufo_launch_count': [P, P],
     'ufo_fp64_peak': [P, P],
+    'ufo_ctx_set_tuning': [P, ctypes.c_int],
+    'ufo_graph_create': [P, P, P, P, P, I64, ctypes.c_int, ctypes.c_int, ctypes.c_int, I64,
+                         ctypes.c_int, P, P, P, P],
+    'ufo_graph_launch': [P, P],
+    'ufo_graph_destroy': [P],
     'ufo_track_noalloc': [P, ctypes.c_int, P, I64, ctypes.c_int, ctypes.c_int, P, P, P, I64,
                           ctypes.c_int, ctypes.c_int, ctypes.c_int, I64, ctypes.c_int, P, P, P,
                           P],
 }
-_VOID = {'ufo_ctx_destroy', 'ufo_prog_destroy'}
+_VOID = {'ufo_ctx_destroy', 'ufo_prog_destroy', 'ufo_graph_destroy'}
 
 
 def load(path=None):

@@ -175,59 +175,97 @@ UFO_DEV void horner_full(const State &s, int n, uint32_t mask, const double *c, 
 }
 
 // trimmed evaluation: za/zb mark exact (structural) zeros
+// One step of the recurrence.  After the top non-zero coefficient m the shape
+// is fixed: the first step (order m) has b == 0 exactly, every later step has
+// both accumulators non-zero; steps differ only in the divisor (1, 2, 4 or a
+// general order) and in whether coefficient order-1 is added.  Each
+// combination is a separate instantiation selected by a switch, so no FP64
+// instruction is predicated.
+template <bool FMA, bool SKEW, bool FIRST, int DK, bool COEF>
+UFO_DEV void hstep(const State &s, double &a, double &b, int order, const double *cp, double o1) {
+  double na, nb;
+  if (FIRST) {  // b is an exact zero
+    na = mul(a, s.x);
+    nb = SKEW ? -mul(a, s.y) : mul(a, s.y);
+  } else if (!SKEW) {
+    na = FMA ? fma_(a, s.x, -mul(b, s.y)) : sub(mul(a, s.x), mul(b, s.y));
+    nb = FMA ? fma_(a, s.y, mul(b, s.x)) : add(mul(a, s.y), mul(b, s.x));
+  } else {
+    na = FMA ? fma_(b, s.y, mul(a, s.x)) : add(mul(b, s.y), mul(a, s.x));
+    nb = FMA ? fma_(b, s.x, -mul(a, s.y)) : sub(mul(b, s.x), mul(a, s.y));
+  }
+  if (DK == 1) {
+    na = mul(na, 0.5);
+    nb = mul(nb, 0.5);
+  } else if (DK == 2) {
+    na = mul(na, 0.25);
+    nb = mul(nb, 0.25);
+  } else if (DK == 3) {
+    const double r = c_rcp_order[order];
+    if (FMA) {
+      na = mul(na, r);
+      nb = mul(nb, r);
+    } else {
+      const double d = static_cast<double>(order);
+      na = divc(na, d, r);
+      nb = divc(nb, d, r);
+    }
+  }
+  if (COEF) {
+    const double cc = ld(cp);  // achromatic: o1 == 1.0 and cc*1.0 == cc exactly
+    a = FMA ? fma_(cc, o1, na) : add(mul(cc, o1), na);
+  } else {
+    a = na;
+  }
+  b = nb;
+}
+
 template <bool FMA, bool SKEW>
 UFO_DEV void horner_trim(const State &s, int n, uint32_t mask, const double *c, bool achro,
                          double &pxd, bool &zpx, double &pyd, bool &zpy) {
-  int k = __popc(mask) - 1;  // index of the top non-zero coefficient in c
-  bool za = !((mask >> (n - 1)) & 1u), zb = true;
-  double a = 0.0, b = 0.0;
-  if (!za) {
-    a = achro ? ld(c + k) : mul(ld(c + k), s.o);
-    --k;
+  (void)n;
+  if (mask == 0u) {
+    pxd = pyd = 0.0;
+    zpx = zpy = true;
+    return;
   }
-  for (int order = n - 1; order > 0; --order) {
-    double na = 0.0, nb = 0.0;
-    const bool zn = za && zb;
-    if (!za && !zb) {
-      if (!SKEW) {
-        na = FMA ? fma_(a, s.x, -mul(b, s.y)) : sub(mul(a, s.x), mul(b, s.y));
-        nb = FMA ? fma_(a, s.y, mul(b, s.x)) : add(mul(a, s.y), mul(b, s.x));
-      } else {
-        na = FMA ? fma_(b, s.y, mul(a, s.x)) : add(mul(b, s.y), mul(a, s.x));
-        nb = FMA ? fma_(b, s.x, -mul(a, s.y)) : sub(mul(b, s.x), mul(a, s.y));
-      }
-    } else if (!za) {  // b is an exact zero
-      na = mul(a, s.x);
-      nb = SKEW ? -mul(a, s.y) : mul(a, s.y);
-    } else if (!zb) {  // a is an exact zero
-      na = SKEW ? mul(b, s.y) : -mul(b, s.y);
-      nb = mul(b, s.x);
+  const int m = 31 - __clz(mask);  // top non-zero coefficient
+  int k = __popc(mask) - 1;        // its index in c
+  const double o1 = achro ? 1.0 : s.o;
+  double a = mul(ld(c + k), o1), b = 0.0;
+  --k;
+  for (int order = m; order > 0; --order) {
+    const int dk = order == 1 ? 0 : order == 2 ? 1 : order == 4 ? 2 : 3;
+    const bool coef = (mask >> (order - 1)) & 1u;
+    const double *cp = c + (k < 0 ? 0 : k);
+    switch ((order == m ? 1 : 0) | (dk << 1) | (coef ? 8 : 0)) {
+      case 0: hstep<FMA, SKEW, false, 0, false>(s, a, b, order, cp, o1); break;
+      case 1: hstep<FMA, SKEW, true, 0, false>(s, a, b, order, cp, o1); break;
+      case 2: hstep<FMA, SKEW, false, 1, false>(s, a, b, order, cp, o1); break;
+      case 3: hstep<FMA, SKEW, true, 1, false>(s, a, b, order, cp, o1); break;
+      case 4: hstep<FMA, SKEW, false, 2, false>(s, a, b, order, cp, o1); break;
+      case 5: hstep<FMA, SKEW, true, 2, false>(s, a, b, order, cp, o1); break;
+      case 6: hstep<FMA, SKEW, false, 3, false>(s, a, b, order, cp, o1); break;
+      case 7: hstep<FMA, SKEW, true, 3, false>(s, a, b, order, cp, o1); break;
+      case 8: hstep<FMA, SKEW, false, 0, true>(s, a, b, order, cp, o1); break;
+      case 9: hstep<FMA, SKEW, true, 0, true>(s, a, b, order, cp, o1); break;
+      case 10: hstep<FMA, SKEW, false, 1, true>(s, a, b, order, cp, o1); break;
+      case 11: hstep<FMA, SKEW, true, 1, true>(s, a, b, order, cp, o1); break;
+      case 12: hstep<FMA, SKEW, false, 2, true>(s, a, b, order, cp, o1); break;
+      case 13: hstep<FMA, SKEW, true, 2, true>(s, a, b, order, cp, o1); break;
+      case 14: hstep<FMA, SKEW, false, 3, true>(s, a, b, order, cp, o1); break;
+      default: hstep<FMA, SKEW, true, 3, true>(s, a, b, order, cp, o1); break;
     }
-    if (!zn) {
-      na = div_order(na, order);
-      nb = div_order(nb, order);
-    }
-    if ((mask >> (order - 1)) & 1u) {
-      const double cc = ld(c + k);
-      --k;
-      if (achro)
-        a = zn ? cc : add(cc, na);
-      else
-        a = zn ? mul(cc, s.o) : (FMA ? fma_(cc, s.o, na) : add(mul(cc, s.o), na));
-      za = false;
-    } else {
-      a = na;
-      za = zn;
-    }
-    b = nb;
-    zb = zn;
+    if (coef) --k;
   }
+  // normal: a = dpx, b = dpy; skew: a = dpy, b = dpx.  b is an exact zero
+  // only when the kick has a single (order 0) coefficient.
   if (!SKEW) {
-    pxd = a; zpx = za;
-    pyd = b; zpy = zb;
+    pxd = a; zpx = false;
+    pyd = b; zpy = (m == 0);
   } else {
-    pxd = b; zpx = zb;
-    pyd = a; zpy = za;
+    pxd = b; zpx = (m == 0);
+    pyd = a; zpy = false;
   }
 }
 

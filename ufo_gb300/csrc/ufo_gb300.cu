@@ -818,3 +818,84 @@ extern "C" int ufo_track_noalloc(const int32_t *ops, int n_ops, const double *d_
                                &d.scratch->queue);
   return launch_kernels(a, needs_full(ops, n_ops), d.sm_count, 16, st);
 }
+
+// ===================================================== tuning and graphs
+
+struct ufo_graph {
+  ufo_ctx *ctx;
+  cudaGraph_t graph;
+  cudaGraphExec_t exec;
+};
+
+extern "C" int ufo_ctx_set_tuning(ufo_ctx *ctx, int warps_per_sm) {
+  if (!ctx) return fail(UFO_E_ARG, "null context");
+  if (warps_per_sm < 1 || warps_per_sm > 32)
+    return fail(UFO_E_ARG, "warps_per_sm %d outside [1, 32]", warps_per_sm);
+  ctx->warps_per_sm = warps_per_sm;
+  return UFO_OK;
+}
+
+// Capture one tracking launch (counter reset + persistent kernel) into a CUDA
+// graph; ufo_graph_launch replays it on the same device buffers.
+extern "C" int ufo_graph_create(ufo_ctx *ctx, const ufo_prog *prog, const double *d_coords,
+                                const int32_t *d_seed, const int32_t *d_pturns, int64_t n,
+                                int turns, int mode, int flags, int64_t slots, int every,
+                                double *d_tracks, uint32_t *d_lost, double *d_final,
+                                ufo_graph **out) {
+  if (!out) return fail(UFO_E_ARG, "null output");
+  *out = nullptr;
+  int rc = check_track_args(ctx, prog, n, turns, mode, slots, every);
+  if (rc) return rc;
+  if (n <= 0) return fail(UFO_E_ARG, "empty launch");
+  if (!d_coords) return fail(UFO_E_ARG, "null coordinates");
+  UFO_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t cap;
+  UFO_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  cudaGraph_t graph = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    rc = launch_track(ctx, prog, d_coords, d_seed, d_pturns, n, turns, mode, flags, slots, every,
+                      d_tracks, d_lost, d_final, cap);
+    e = cudaStreamEndCapture(cap, &graph);
+  }
+  cudaStreamDestroy(cap);
+  if (rc) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "stream capture");
+  cudaGraphExec_t exec = nullptr;
+  e = cudaGraphInstantiate(&exec, graph, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(graph);
+    return cuda_fail(e, "cudaGraphInstantiate");
+  }
+  ufo_graph *g = new (std::nothrow) ufo_graph;
+  if (!g) {
+    cudaGraphExecDestroy(exec);
+    cudaGraphDestroy(graph);
+    return fail(UFO_E_NOMEM, "host allocation");
+  }
+  g->ctx = ctx;
+  g->graph = graph;
+  g->exec = exec;
+  *out = g;
+  return UFO_OK;
+}
+
+extern "C" int ufo_graph_launch(ufo_graph *g, void *stream) {
+  if (!g) return fail(UFO_E_ARG, "null graph");
+  UFO_CUDA(cudaSetDevice(g->ctx->device));
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : g->ctx->stream;
+  UFO_CUDA(cudaGraphLaunch(g->exec, st));
+  g->ctx->launches.fetch_add(1);
+  return UFO_OK;
+}
+
+extern "C" void ufo_graph_destroy(ufo_graph *g) {
+  if (!g) return;
+  cudaSetDevice(g->ctx->device);
+  cudaGraphExecDestroy(g->exec);
+  cudaGraphDestroy(g->graph);
+  delete g;
+}
