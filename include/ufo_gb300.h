@@ -140,6 +140,30 @@ int ufo_graph_create(ufo_ctx *ctx, const ufo_prog *prog, const double *d_coords,
 int ufo_graph_launch(ufo_graph *graph, void *stream);
 void ufo_graph_destroy(ufo_graph *graph);
 
+/*
+ * Tangent map and adjoint of the one-turn map (no reference counterpart: the
+ * reference differentiates only by finite differences of tunes in dp,
+ * tests/optics3.py:13-23).  Device pointers throughout, asynchronous on
+ * `stream`; 0 on success, -1 bad argument, -2 launch error.  `ops` is the
+ * differentiator's opcode list int32[n_ops][8] and `tab` its constants (built
+ * by ufo_gb300/diff.py), one row of `tab_stride` constants per seed, `seed`
+ * int32[J] the row of each job (NULL: row 0); one job per thread.
+ *   ufo_diff_forward: z0 f64[J][4], o f64[J] (1/(1+dp)) -> zT f64[J][20]
+ *     (state and, with `tangent`, the 4x4 Jacobian), checkpoints f64[J][turns/ck+1][20]
+ *   ufo_diff_reverse: output cotangents zbar f64[J][4] (and Tbar f64[J][16])
+ *     -> zbar0 f64[J][4], parameter cotangents pbar f64[J][n_params]; scratch
+ *     seg f64[J][ck][20] and tape f64[J][kicks_per_turn][10].
+ */
+int ufo_diff_forward(const int32_t *ops, int n_ops, const double *tab, int64_t tab_stride,
+                     const int32_t *seed, int n_params, int kicks_per_turn, int n_jobs,
+                     const double *z0, const double *o, int turns, int ck, int tangent,
+                     double *ckpt, double *zT, void *stream);
+int ufo_diff_reverse(const int32_t *ops, int n_ops, const double *tab, int64_t tab_stride,
+                     const int32_t *seed, int n_params, int kicks_per_turn, int n_jobs,
+                     const double *o, int turns, int ck, int tangent, const double *ckpt,
+                     const double *zbar, const double *Tbar, double *seg, double *tape,
+                     double *zbar0, double *pbar, void *stream);
+
 /* Kernel launches issued by this library since the context was created.
  * Diagnostic; no reference counterpart. */
 int ufo_launch_count(ufo_ctx *ctx, int64_t *count);

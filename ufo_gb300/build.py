@@ -14,7 +14,7 @@ ROOT = os.path.dirname(HERE)
 SRC = os.path.join(HERE, 'csrc')
 OUT_DIR = os.path.join(HERE, 'lib')
 SO = os.path.join(OUT_DIR, 'libufo_gb300.so')
-SOURCES = ['ufo_gb300.cu']
+SOURCES = ['ufo_gb300.cu', 'diff.cu']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 NVCC_FLAGS = ['-O3', '-lineinfo', '-std=c++17', '-shared', '-Xcompiler', '-fPIC',
               '-I', os.path.join(ROOT, 'include')]

@@ -251,3 +251,40 @@ def c2_ring(m, seed=2, slices=4):
         rng.bit_generator.state = st
         cells.extend(_c2_cell(m, c, rng, slices))
     return m.Line('RING', cells)
+
+
+# ----------------------------------------------------------------- C5
+
+def c5_ring(m, seed=5, slices=4):
+    """C5: the C2 ring with one C4-style error seed on every magnet (dx, dy ~
+    N(0, 50 um); normal and skew errors of MAD orders 3..6 relative to the
+    main field at r0 = 10 mm)."""
+    ring = c2_ring(m, slices=slices)
+    rng = np.random.default_rng(seed)
+    for e in ring.flatten():
+        t = type(e).__name__
+        if t not in ('Quadrupole', 'Sbend', 'Sextupole'):
+            continue
+        if t == 'Quadrupole':
+            kmain, mo = abs(e.k1), 1
+        elif t == 'Sextupole':
+            kmain, mo = abs(e.k2), 2
+        else:
+            kmain, mo = abs(e.angle / e.length), 0
+        e.dx, e.dy = rng.normal(0, 50e-6), rng.normal(0, 50e-6)
+        e.dkn = [0.0] * 6
+        e.dks = [0.0] * 6
+        for j in range(2, 6):
+            e.dkn[j] = rng.normal(0, 1e-4) * kmain / R0 ** (j - mo)
+            e.dks[j] = rng.normal(0, 1e-4) * kmain / R0 ** (j - mo)
+    return ring
+
+
+def c5_parameters(ring):
+    """The 320 quadrupole k1 and 192 sextupole k2 of the C5 ring (flat index,
+    attribute) and their values."""
+    flat = ring.flatten()
+    q = [(i, 'k1') for i, e in enumerate(flat) if type(e).__name__ == 'Quadrupole']
+    s = [(i, 'k2') for i, e in enumerate(flat) if type(e).__name__ == 'Sextupole']
+    vals = [flat[i].k1 for i, _ in q] + [flat[i].k2 for i, _ in s]
+    return q + s, np.array(vals, dtype=np.float64)
