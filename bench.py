@@ -51,9 +51,13 @@ def parse():
     ap.add_argument('--particles', type=int, default=65536)
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
-    ap.add_argument('--workload', default='c2', choices=['c2', 'c4'])
+    ap.add_argument('--workload', default='c2', choices=['c2', 'c4', 'c5'])
     ap.add_argument('--seeds', type=int, default=64, help='C4: number of seeds')
     ap.add_argument('--turn-div', type=int, default=4, help='C4: divide turn counts by this')
+    ap.add_argument('--c5-seeds', type=int, default=256,
+                    help='C5: error seeds in the GPU-filling adjoint batch')
+    ap.add_argument('--c5-fd-params', type=int, default=8,
+                    help='C5: parameters in the sampled multi-turn FD')
     return ap.parse_args()
 
 
@@ -400,6 +404,201 @@ def bench_c4(args):
     print(json.dumps(line), flush=True)
 
 
+def _normwise(g, fd):
+    """max |g - fd| / max |fd| per output row."""
+    g, fd = np.atleast_2d(g), np.atleast_2d(fd)
+    return (np.max(np.abs(g - fd), axis=1) / np.max(np.abs(fd), axis=1)).tolist()
+
+
+def bench_c5(args):
+    """Adjoint gradients (C5: the C2 ring with one error seed, 320 k1 + 192 k2)
+    against central finite differences, accuracy over all 512 parameters and
+    cost in device time (CUDA events around every kernel) and wall time:
+      optics_one_seed    the 8 x 512 Jacobian of (closed orbit, Qx, Qy, xi_x,
+                         xi_y): adjoint = Newton + one vjp launch pair for all
+                         8 cotangents; FD = 1,024 perturbed rows batched into
+                         one Newton job list (h = 1e-7 relative), plus a
+                         4-point stencil (h = 1e-5, xi: 1e-4) as the tighter
+                         check
+      optics_batched     the same Jacobians for many error seeds, each method
+                         batched until the GPU is full (adjoint: --c5-seeds
+                         seeds; FD: 2 seeds = 2,048 rows), cost per Jacobian
+      multiturn          d/dk of sum(x^2 + y^2) of 4,096 particles after 1,024
+                         turns (particles on chaotic orbits masked out),
+                         checkpoints every 64 turns; FD = batched
+                         tracking of 2 x --c5-fd-params perturbed rings (4,096
+                         particles each) through the persistent tracking
+                         kernel, scaled to all 512 parameters
+    """
+    import torch
+    import ufo_gb300 as u
+    from ufo_gb300 import diff as D, workloads as W
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)  # every kernel below and its events on one stream
+    ctx = u.context(0)
+    ring = W.c5_ring(u)
+    params, vals = W.c5_parameters(ring)
+    P = len(vals)
+    model = D.OpticsModel(ring, u.KICK, params, h_dp=1e-5)
+    clocks = Clocks(0)
+    clocks.start()
+    model.evaluate(vals)  # warm-up
+    res = {}
+    launches = 0
+
+    # ---- one seed: full Jacobian
+    t0 = time.perf_counter()
+    out, saved = model.evaluate(vals)
+    Jad = model.vjp(saved, np.eye(8))
+    wall_adj = time.perf_counter() - t0
+    dev_adj = saved[0].device_ms
+    launches += saved[0].launches
+
+    def fd_rows(hrel, stencil):
+        h = hrel * np.abs(vals)
+        rows = np.repeat(vals[None], len(stencil) * P, 0)
+        for j, c in enumerate(stencil):
+            rows[j::len(stencil)][np.arange(P), np.arange(P)] += c * h
+        return rows, h
+
+    rows, h = fd_rows(1e-7, (1, -1))
+    t0 = time.perf_counter()
+    fo, fs = model.evaluate_batch(rows)
+    wall_fd = time.perf_counter() - t0
+    dev_fd = fs[0].device_ms
+    launches += fs[0].launches
+    Jfd = ((fo[0::2] - fo[1::2]) / (2 * h[:, None])).T
+    rows4, h4 = fd_rows(1e-5, (2, 1, -1, -2))
+    rows4x, h4x = fd_rows(1e-4, (2, 1, -1, -2))
+    f4 = model.evaluate_many(rows4)
+    f4x = model.evaluate_many(rows4x)
+
+    def st4(f, hh):
+        return ((-f[0::4] + 8 * f[1::4] - 8 * f[2::4] + f[3::4]) / (12 * hh[:, None])).T
+
+    J4 = st4(f4, h4)
+    J4[6:8] = st4(f4x, h4x)[6:8]
+    names = ['x_co', 'px_co', 'y_co', 'py_co', 'Qx', 'Qy', 'xi_x', 'xi_y']
+    res['optics_one_seed'] = {
+        'outputs': dict(zip(names, out.tolist())),
+        'adjoint_device_ms': dev_adj, 'adjoint_wall_s': wall_adj,
+        'fd_device_ms': dev_fd, 'fd_wall_s': wall_fd,
+        'device_cost_ratio': dev_fd / dev_adj, 'wall_cost_ratio': wall_fd / wall_adj,
+        'normwise_rel_err_vs_central_fd_h1e-7': dict(zip(names, _normwise(Jad, Jfd))),
+        'normwise_rel_err_vs_4pt_fd': dict(zip(names, _normwise(Jad, J4))),
+        'note': 'one seed leaves the GPU mostly idle: the 3,072 FD Newton jobs run '
+                'beside each other in the time of the 3 adjoint jobs'}
+
+    # ---- GPU-filling batches: cost per 8 x 512 Jacobian
+    rng = np.random.default_rng(55)
+    Sa = args.c5_seeds
+    rows_a = vals[None] * (1 + 1e-3 * rng.standard_normal((Sa, P)))
+    t0 = time.perf_counter()
+    oa, sa = model.evaluate_batch(rows_a)
+    Ka = model.vjp(sa, np.repeat(np.eye(8)[None], Sa, 0))
+    wall_a = time.perf_counter() - t0
+    dev_a = sa[0].device_ms
+    launches += sa[0].launches
+    Sf = 2
+    rows_f = np.concatenate([fd_rows(1e-7, (1, -1))[0] * (r / vals)[None]
+                             for r in rows_a[:Sf]])
+    t0 = time.perf_counter()
+    of, sf = model.evaluate_batch(rows_f)
+    wall_f = time.perf_counter() - t0
+    dev_f = sf[0].device_ms
+    launches += sf[0].launches
+    res['optics_batched'] = {
+        'adjoint_seeds': Sa, 'fd_seeds': Sf,
+        'adjoint_device_ms_per_jacobian': dev_a / Sa, 'fd_device_ms_per_jacobian': dev_f / Sf,
+        'adjoint_wall_ms_per_jacobian': 1e3 * wall_a / Sa,
+        'fd_wall_ms_per_jacobian': 1e3 * wall_f / Sf,
+        'device_cost_ratio': (dev_f / Sf) / (dev_a / Sa),
+        'wall_cost_ratio': (wall_f / Sf) / (wall_a / Sa)}
+
+    # ---- multi-turn amplitude adjoint
+    Np, T, ck = 4096, 1024, 64
+    coords = W.c2_beam(Np, seed=3)
+    o = 1.0 / (coords[:, 5] + 1.0)
+    eng = model.engine(vals)
+    # particles on chaotic (resonant) orbits have no usable derivative over
+    # 1,024 turns: a 1e-9 m displacement grows exponentially there.  They are
+    # excluded from the objective (a fixed mask, not differentiated).
+    pair = np.concatenate([coords[:, :4], coords[:, :4] + [1e-9, 0, 0, 0]])
+    zp, _ = eng.forward(pair, np.concatenate([o, o]), T)
+    growth = np.max(np.abs(zp[Np:, :4] - zp[:Np, :4]), axis=1) / 1e-9
+    mask = growth < 1e4
+    eng.device_ms, eng.launches = 0.0, 0
+    t0 = time.perf_counter()
+    zT, st = eng.forward(coords[:, :4], o, T, ck=ck)
+    zbar = np.zeros((Np, 4))
+    zbar[:, 0] = 2 * zT[:, 0] * mask
+    zbar[:, 2] = 2 * zT[:, 2] * mask
+    _, gp = eng.reverse(st, zbar)  # per particle [Np, P]
+    g = gp.sum(axis=0)
+    wall_mt = time.perf_counter() - t0
+    dev_mt = eng.device_ms
+    launches += eng.launches
+    del st
+    torch.cuda.empty_cache()
+    m = args.c5_fd_params
+    idx = np.sort(rng.choice(P, m, replace=False))
+    hm = 1e-7 * np.abs(vals[idx])
+    rows_m = np.repeat(vals[None], 2 * m, 0)
+    rows_m[0::2][np.arange(m), idx] += hm
+    rows_m[1::2][np.arange(m), idx] -= hm
+    b = u.TrackBatch(ring, params, rows_m, [Np] * (2 * m), [T] * (2 * m),
+                     flags=u.KICK | u.FMA, context=ctx)
+    b.coords[:] = np.tile(coords, (2 * m, 1))
+    b.upload()
+    b.capture()
+    b.launch(stream=stream.cuda_stream)  # warm-up (graph upload)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = ctx.launches()
+    e0.record(stream)
+    b.launch(stream=stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches += ctx.launches() - l0
+    dev_fdm = e0.elapsed_time(e1)
+    fin, lost = b.download()
+    ampp = (fin[:, 0] ** 2 + fin[:, 2] ** 2).reshape(2 * m, Np) * mask[None]
+    fdp = (ampp[0::2] - ampp[1::2]) / (2 * hm[:, None])  # per particle [m, Np]
+    fdm = fdp.sum(axis=1)
+    rel = np.abs(g[idx] - fdm) / np.abs(fdp).sum(axis=1)
+    pp = np.abs(gp[:, idx].T - fdp)[:, mask] / np.maximum(np.abs(fdp[:, mask]), 1e-300)
+    fd_full = dev_fdm * P / m
+    res['multiturn'] = {
+        'particles': Np, 'turns': T, 'checkpoint_every': ck,
+        'regular_particles': int(mask.sum()),
+        'adjoint_device_ms': dev_mt, 'adjoint_wall_s': wall_mt,
+        'fd_sample_params': m, 'fd_sample_device_ms': dev_fdm,
+        'fd_all_params_device_ms_scaled': fd_full,
+        'device_cost_ratio': fd_full / dev_mt,
+        'fd_lost_particles': int(np.sum(lost < T)),
+        'growth_quantiles_50_99_max': np.quantile(growth, [0.5, 0.99, 1.0]).tolist(),
+        'max_rel_err_vs_central_fd_h1e-7': float(rel.max()),
+        'rel_err_per_param': rel.tolist(),
+        'rel_err_note': '|sum(adjoint - FD)| / sum|per-particle FD| over the regular '
+                        'particles; FD through the tracking kernel (FMA mode)',
+        'per_particle_median_rel_err': float(np.median(pp))}
+    clk = clocks.stop()
+    ratio = min(res['optics_batched']['device_cost_ratio'], res['multiturn']['device_cost_ratio'])
+    line = {'metric': 'adjoint gradient cost advantage over central finite differences '
+                      '(device time, all 512 parameters)',
+            'value': ratio, 'unit': 'x', 'n_gpus': 1, 'steps': 1, 'warmup': 1,
+            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+            'data': 'synthetic',
+            'config': {'workload': 'C5 adjoint optics gradients: C2 ring (1024 elements) with '
+                                   'one error seed, d/d(320 k1 + 192 k2) of closed orbit, '
+                                   'tunes, chromaticity; 4096-particle 1024-turn amplitude '
+                                   'adjoint with checkpoints every 64 turns'},
+            'gpu_launches': launches, 'clocks': clk}
+    line.update(res)
+    print(json.dumps(line), flush=True)
+
+
 def ctypes_peak(ctx):
     import ctypes
     from ufo_gb300 import capi
@@ -414,6 +613,8 @@ def main():
         bench_reference(args)
     elif args.workload == 'c4':
         bench_c4(args)
+    elif args.workload == 'c5':
+        bench_c5(args)
     else:
         bench_ours(args)
 

@@ -149,10 +149,12 @@ void ufo_graph_destroy(ufo_graph *graph);
  * by ufo_gb300/diff.py), one row of `tab_stride` constants per seed, `seed`
  * int32[J] the row of each job (NULL: row 0); one job per thread.
  *   ufo_diff_forward: z0 f64[J][4], o f64[J] (1/(1+dp)) -> zT f64[J][20]
- *     (state and, with `tangent`, the 4x4 Jacobian), checkpoints f64[J][turns/ck+1][20]
- *   ufo_diff_reverse: output cotangents zbar f64[J][4] (and Tbar f64[J][16])
- *     -> zbar0 f64[J][4], parameter cotangents pbar f64[J][n_params]; scratch
- *     seg f64[J][ck][20] and tape f64[J][kicks_per_turn][10].
+ *     (state and, with `tangent`, the 4x4 Jacobian), checkpoints
+ *     f64[turns/ck+1][20][J] every `ck` turns (NULL: none)
+ *   ufo_diff_reverse: the checkpoints of the forward call, output cotangents
+ *     zbar f64[J][4] (and Tbar f64[J][16]) -> zbar0 f64[J][4], parameter
+ *     cotangents pbar f64[n_params][J]; scratch tape
+ *     f64[ck][kicks_per_turn][nf][J], nf = 10 with `tangent`, else 2.
  */
 int ufo_diff_forward(const int32_t *ops, int n_ops, const double *tab, int64_t tab_stride,
                      const int32_t *seed, int n_params, int kicks_per_turn, int n_jobs,
@@ -161,8 +163,8 @@ int ufo_diff_forward(const int32_t *ops, int n_ops, const double *tab, int64_t t
 int ufo_diff_reverse(const int32_t *ops, int n_ops, const double *tab, int64_t tab_stride,
                      const int32_t *seed, int n_params, int kicks_per_turn, int n_jobs,
                      const double *o, int turns, int ck, int tangent, const double *ckpt,
-                     const double *zbar, const double *Tbar, double *seg, double *tape,
-                     double *zbar0, double *pbar, void *stream);
+                     const double *zbar, const double *Tbar, double *tape, double *zbar0,
+                     double *pbar, void *stream);
 
 /* Kernel launches issued by this library since the context was created.
  * Diagnostic; no reference counterpart. */

@@ -147,3 +147,85 @@ def test_batched_optics_match_single_evaluations():
     for s in range(3):
         one, _ = model.evaluate(rows[s])
         assert np.array_equal(many[s], one)
+
+
+def test_vjp_rows_match_single_vjps():
+    """[S, R, 8] cotangent blocks (several seeds, several cotangents each) give
+    the same parameter cotangents as one vjp per (seed, cotangent)."""
+    import ufo_gb300 as u
+    from ufo_gb300 import diff as D
+    ring = _ring()
+    params, vals = _params(ring)
+    model = D.OpticsModel(ring, u.KICK, params)
+    rng = np.random.default_rng(11)
+    rows = vals[None] * (1 + 1e-3 * rng.standard_normal((2, len(vals))))
+    G = rng.standard_normal((2, 3, 8))
+    out, saved = model.evaluate_batch(rows)
+    K = model.vjp(saved, G)
+    assert K.shape == (2, 3, len(vals))
+    for s in range(2):
+        o1, sv1 = model.evaluate(rows[s])
+        assert np.array_equal(o1, out[s])
+        for r in range(3):
+            k1 = model.vjp(sv1, G[s, r])
+            np.testing.assert_allclose(K[s, r], k1, rtol=1e-13, atol=1e-13 * np.abs(k1).max())
+
+
+def _linear_ring():
+    """The C2 ring without its apertures (the reference's optics method tracks
+    unit particles at 1 m amplitude)."""
+    import ufo_gb300 as u
+    from ufo_gb300 import workloads as W
+    ring = W.c2_ring(u)
+    return u.Line('RING', [e for e in ring.flatten() if type(e).__name__ != 'Aperture'])
+
+
+def test_tunes_and_gradients_vs_reference_optics_method():
+    """Against the reference's own machinery: the Optics driver (unit-particle
+    linear-map columns, ufo/optics.py:96-103, bit-exact with the reference's
+    kernel) in LINEAR mode with a DOUBLE_PRECISION parameter pool (without it
+    the pool, like the reference's, is float32).  The origin is the closed
+    orbit of this error-free ring, so the unit-particle columns are the map:
+    tunes agree to rounding; adjoint dQ/dk1 agrees with central differences of
+    the Optics tunes; the chromaticity agrees with the reference's one-sided dp
+    difference (tests/optics3.py, delta 1e-4) to that method's own truncation
+    and affine-offset error."""
+    import torch
+    import ufo_gb300 as u
+    from ufo_gb300 import diff as D
+    ring = _linear_ring()
+    flat = ring.flatten()
+    quads = [i for i, e in enumerate(flat) if type(e).__name__ == 'Quadrupole']
+    params = [(i, 'k1') for i in quads]
+    vals = np.array([flat[i].k1 for i in quads])
+    flags = u.KICK | u.LINEAR | u.DOUBLE_PRECISION
+    model = D.OpticsModel(ring, flags, params)
+    k = torch.tensor(vals, dtype=torch.float64, requires_grad=True)
+    out = D.optics(k, model)
+    out[4].backward()
+    g = k.grad.numpy()
+    o = u.Optics(ring, where=[], parameters=params + ['dp'], flags=flags)
+
+    def tunes(v, dp=0.0):
+        o.parameters[0, :len(v)] = v
+        o.parameters[0, -1] = dp
+        o.run()
+        return o.qx, o.qy
+
+    qx, qy = tunes(vals)
+    assert np.max(np.abs(out[:4].detach().numpy())) < 1e-15
+    assert abs(out[4].item() - qx) < 1e-12 and abs(out[5].item() - qy) < 1e-12
+    rng = np.random.default_rng(5)
+    scale = np.abs(g).max()
+    for i in rng.choice(len(vals), 8, replace=False):
+        h = 1e-7 * abs(vals[i])
+        vp, vm = vals.copy(), vals.copy()
+        vp[i] += h
+        vm[i] -= h
+        fd = (tunes(vp)[0] - tunes(vm)[0]) / (2 * h)
+        assert abs(g[i] - fd) <= 1e-6 * max(abs(fd), 1e-6 * scale) + 1e-14 / (2 * h), (i, g[i], fd)
+    d = 1e-4
+    q1 = tunes(vals, d)
+    xi_ref = [(q1[0] - qx) / d, (q1[1] - qy) / d]
+    xi = out[6:8].detach().numpy()
+    assert np.all(np.abs(xi - xi_ref) <= 1e-2 * np.abs(xi)), (xi, xi_ref)

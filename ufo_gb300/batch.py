@@ -180,7 +180,7 @@ class TrackBatch:
         return self.download()
 
     def destroy_graph(self):
-        if self._graph is not None and capi._lib is not None:
+        if self._graph is not None and capi.alive():
             capi._lib.ufo_graph_destroy(self._graph)
         self._graph = None
 

@@ -3,6 +3,7 @@
 The library is required: there is no CPU fallback.  If it is missing or fails
 to load, every GPU entry point raises ``RuntimeError``.
 """
+import atexit
 import ctypes
 import os
 import threading
@@ -17,6 +18,20 @@ UFO_TRACK_FMA, UFO_TRACK_FIVED, UFO_TRACK_PLAIN = 1, 2, 4
 
 _lib = None
 _lock = threading.Lock()
+_exiting = False  # set at interpreter exit: destructors then leave teardown to the driver
+
+
+def _mark_exit():
+    global _exiting
+    _exiting = True
+
+
+atexit.register(_mark_exit)
+
+
+def alive():
+    """True while native handles may still be released."""
+    return _lib is not None and not _exiting
 
 P = ctypes.c_void_p
 I32, I64, D = ctypes.c_int32, ctypes.c_int64, ctypes.c_double
@@ -44,7 +59,7 @@ SIGNATURES = {
     'ufo_diff_forward': [P, ctypes.c_int, P, I64, P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                          P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P],
     'ufo_diff_reverse': [P, ctypes.c_int, P, I64, P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                         P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P, P],
+                         P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P],
     'ufo_track_noalloc': [P, ctypes.c_int, P, I64, ctypes.c_int, ctypes.c_int, P, P, P, I64,
                           ctypes.c_int, ctypes.c_int, ctypes.c_int, I64, ctypes.c_int, P, P, P,
                           P],
@@ -110,7 +125,7 @@ class Context:
 
     def __del__(self):
         h = getattr(self, 'handle', None)
-        if h and _lib is not None:
+        if h and alive():
             _lib.ufo_ctx_destroy(h)
             self.handle = None
 
@@ -138,7 +153,7 @@ class DeviceProgram:
 
     def __del__(self):
         h = getattr(self, 'handle', None)
-        if h and _lib is not None:
+        if h and alive():
             _lib.ufo_prog_destroy(h)
             self.handle = None
 

@@ -4,21 +4,26 @@
 // the compiled line): drifts, teapot elements, thin kicks, alignments and
 // constant edges.  Every kick of the reference (ufo/methods.py:45-76, the
 // Horner scheme) is the complex polynomial
-//     S(z) = o * sum_n (c_n + i s_n) z^n / n!,   z = x + i y,
+//     S(z) = o * sum_n (a_n + i b_n) z^n,   z = x + i y,
+//     a_n = kn_n / n!,  b_n = ks_n / n!,
 //     px -= Re S,   py += Im S,
-// so its derivatives follow from S' and S'' (Cauchy-Riemann).  A teapot slice is
-// kick, weak focusing (px -= W x), drift.  Element strengths enter linearly:
-// one parameter per element scales coefficient `pm` with dK/dk (= L*f/N).
+// so its derivatives follow from S' and S'' (Cauchy-Riemann); one Horner pass
+// gives S, S' and S''/2 together.  A teapot slice is kick, weak focusing
+// (px -= W x), drift.  Element strengths enter linearly: one parameter per
+// element scales coefficient `pm`; the table carries dK/dk / pm! and
+// dK/dk / (pm-1)! for the S and S' terms.
 //
 // diff_forward: z (and optionally the 4x4 tangent T = dz/dz0) through `turns`
 //   turns, writing the state (and T) every `ck` turns as checkpoints.
-// diff_reverse: given the output cotangents zbar (and Tbar), walks the turns
-//   backwards: each checkpoint segment is re-tracked once to recover its turn
-//   starts, each turn is re-tracked onto a tape (x, y and the x/y rows of T at
-//   every kick) and then reversed; accumulates the cotangent of the start state
+// diff_reverse: given the output cotangents zbar (and Tbar), walks the
+//   checkpoint segments backwards: each segment is re-tracked once onto a tape
+//   (x, y and the x/y rows of T at every kick of every turn of the segment) and
+//   then reversed turn by turn; accumulates the cotangent of the start state
 //   and of every element parameter.
-// Arithmetic is FP64 with fused multiply-adds (gradients need FP64 accuracy,
-// not the reference's rounding).  One thread per job.
+// Per-job buffers that grow with the work (checkpoints, tape, parameter
+// cotangents) are laid out job-fastest, so a warp's 32 jobs touch 32
+// consecutive doubles.  Arithmetic is FP64 with fused multiply-adds (gradients
+// need FP64 accuracy, not the reference's rounding).  One thread per job.
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -26,7 +31,7 @@
 namespace ufo_diff {
 
 enum : int { D_NOP = 0, D_DRIFT, D_TEAPOT, D_KICK, D_ALIGN, D_EDGE };
-constexpr int MAXC = 16;  // multipole orders handled by the differentiator
+constexpr int KHDR = 5;   // kick constants: Lo, Li, W, g0, g1, then a[M], b[M]
 
 struct DOp {
   int kind, flags, toff, N, M, pslot, pm, achro;
@@ -45,14 +50,13 @@ struct DiffArgs {
   const double *o;        // [job] 1/(1+dp)
   int turns, ck;          // turns, checkpoint interval
   int tangent;            // propagate T
-  double *ckpt;           // [job][turns/ck + 1][20]
+  double *ckpt;           // [turns/ck + 1][20][job]
   double *zT;             // [job][20] final state (+T)
   const double *zbar;     // [job][4] output cotangents
   const double *Tbar;     // [job][16] (tangent only)
-  double *seg;            // [job][ck][20] turn starts of one segment
-  double *tape;           // [job][kicks_per_turn][10]
+  double *tape;           // [ck][kicks_per_turn][nf][job], nf = 10 (tangent) or 2
   double *zbar0;          // [job][4] cotangent of the start state
-  double *pbar;           // [job][n_params]
+  double *pbar;           // [n_params][job]
 };
 
 struct St {
@@ -60,48 +64,38 @@ struct St {
   double T[16];  // rows x, px, y, py; columns = start coordinates
 };
 
-__device__ __forceinline__ double fact(int n) {
-  double f = 1.0;
-  for (int k = 2; k <= n; ++k) f *= k;
-  return f;
-}
-
-// S^(d)(z) / o for d = 0, 1, 2: sum_n C_n z^(n-d) / (n-d)!
-__device__ void poly(const double *cr, const double *ci, int M, double x, double y, int d,
-                     double &re, double &im) {
-  re = 0.0;
-  im = 0.0;
-  for (int n = M - 1; n >= d; --n) {  // Horner in z with the 1/(n-d)! weights
-    const double w = 1.0 / fact(n - d);
-    const double tr = fma(re, x, -im * y), ti = fma(re, y, im * x);
-    re = tr + cr[n] * w;
-    im = ti + ci[n] * w;
-  }
-}
-
-__device__ __forceinline__ void fwd_kick(St &s, const double *cr, const double *ci, int M,
-                                         double o, bool tangent) {
-  double sr, si;
-  poly(cr, ci, M, s.x, s.y, 0, sr, si);
-  if (tangent) {
-    double a, b;
-    poly(cr, ci, M, s.x, s.y, 1, a, b);
-    a *= o;
-    b *= o;
-    for (int j = 0; j < 4; ++j) {
-      const double dx = s.T[j], dy = s.T[8 + j];
-      s.T[4 + j] -= fma(a, dx, -b * dy);
-      s.T[12 + j] += fma(b, dx, a * dy);
+// S(z)/o, S'(z)/o and S''(z)/(2o) by one Horner pass over the power series
+// (ND = highest derivative wanted)
+template <int ND>
+__device__ __forceinline__ void series(const double *__restrict__ a, int M, double x, double y,
+                                       double &s0r, double &s0i, double &s1r, double &s1i,
+                                       double &s2r, double &s2i) {
+  const double *b = a + M;
+  s0r = __ldg(a + M - 1);
+  s0i = __ldg(b + M - 1);
+  s1r = s1i = s2r = s2i = 0.0;
+  for (int n = M - 2; n >= 0; --n) {
+    if (ND >= 2) {
+      const double tr = fma(s2r, x, fma(-s2i, y, s1r));
+      s2i = fma(s2r, y, fma(s2i, x, s1i));
+      s2r = tr;
     }
+    if (ND >= 1) {
+      const double tr = fma(s1r, x, fma(-s1i, y, s0r));
+      s1i = fma(s1r, y, fma(s1i, x, s0i));
+      s1r = tr;
+    }
+    const double tr = fma(s0r, x, fma(-s0i, y, __ldg(a + n)));
+    s0i = fma(s0r, y, fma(s0i, x, __ldg(b + n)));
+    s0r = tr;
   }
-  s.px -= o * sr;
-  s.py += o * si;
 }
 
 __device__ __forceinline__ void fwd_drift(St &s, double L, bool tangent) {
   s.x = fma(s.px, L, s.x);
   s.y = fma(s.py, L, s.y);
   if (tangent)
+#pragma unroll
     for (int j = 0; j < 4; ++j) {
       s.T[j] = fma(s.T[4 + j], L, s.T[j]);
       s.T[8 + j] = fma(s.T[12 + j], L, s.T[8 + j]);
@@ -111,43 +105,62 @@ __device__ __forceinline__ void fwd_drift(St &s, double L, bool tangent) {
 __device__ __forceinline__ void fwd_weak(St &s, double W, bool tangent) {
   s.px = fma(-W, s.x, s.px);
   if (tangent)
+#pragma unroll
     for (int j = 0; j < 4; ++j) s.T[4 + j] = fma(-W, s.T[j], s.T[4 + j]);
 }
 
-// teapot constants: [Lo, Li, W, dKdk, cr[M], ci[M]]
-__device__ void load_coefs(const double *c, int M, double *cr, double *ci) {
-  for (int n = 0; n < MAXC; ++n) {
-    cr[n] = n < M ? c[n] : 0.0;
-    ci[n] = n < M ? c[M + n] : 0.0;
+__device__ __forceinline__ void fwd_kick(St &s, const double *a, int M, double o, bool tangent) {
+  double sr, si, ar, ai, br, bi;
+  if (tangent) {
+    series<1>(a, M, s.x, s.y, sr, si, ar, ai, br, bi);
+    ar *= o;
+    ai *= o;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const double dx = s.T[j], dy = s.T[8 + j];
+      s.T[4 + j] -= fma(ar, dx, -ai * dy);
+      s.T[12 + j] += fma(ai, dx, ar * dy);
+    }
+  } else {
+    series<0>(a, M, s.x, s.y, sr, si, ar, ai, br, bi);
   }
+  s.px -= o * sr;
+  s.py += o * si;
 }
 
-// one turn forward; with `tape` the state at every kick is recorded
+// tape slot of field f of kick k in turn tt of the segment
+__device__ __forceinline__ int64_t tidx(const DiffArgs &a, int tt, int k, int f, int nf, int j) {
+  return ((static_cast<int64_t>(tt) * a.kicks_per_turn + k) * nf + f) * a.n_jobs + j;
+}
+
+// one turn forward; with `tape` the state at every kick is recorded as turn
+// `tt` of the segment
 __device__ void turn_forward(St &s, const DiffArgs &a, const double *T0, double o, bool tangent,
-                             double *tape) {
+                             int j, int tt, bool tape) {
   int kidx = 0;
-  double cr[MAXC], ci[MAXC];
+  const int nf = tangent ? 10 : 2;
   for (int i = 0; i < a.n_ops; ++i) {
     const DOp op = a.ops[i];
     const double *c = T0 + op.toff;
     const double oo = op.achro ? 1.0 : o;
     switch (op.kind) {
       case D_DRIFT:
-        fwd_drift(s, c[0], tangent);
+        fwd_drift(s, __ldg(c), tangent);
         break;
       case D_ALIGN:
-        s.x -= c[0];
-        s.y -= c[1];
+        s.x -= __ldg(c);
+        s.y -= __ldg(c + 1);
         break;
       case D_EDGE: {
-        const double curv = c[0] * oo;
+        const double curv = __ldg(c) * oo, e1 = __ldg(c + 1), e2 = __ldg(c + 2);
         const double x0 = s.x, y0 = s.y;
-        s.px = fma(x0 * curv, c[1], s.px);
-        s.py = fma(-(y0 * curv), c[2], s.py);
+        s.px = fma(x0 * curv, e1, s.px);
+        s.py = fma(-(y0 * curv), e2, s.py);
         if (tangent)
-          for (int j = 0; j < 4; ++j) {
-            s.T[4 + j] = fma(s.T[j] * curv, c[1], s.T[4 + j]);
-            s.T[12 + j] = fma(-(s.T[8 + j] * curv), c[2], s.T[12 + j]);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            s.T[4 + q] = fma(s.T[q] * curv, e1, s.T[4 + q]);
+            s.T[12 + q] = fma(-(s.T[8 + q] * curv), e2, s.T[12 + q]);
           }
         break;
       }
@@ -155,21 +168,22 @@ __device__ void turn_forward(St &s, const DiffArgs &a, const double *T0, double 
       case D_TEAPOT: {
         const bool tp = op.kind == D_TEAPOT;
         const int N = tp ? op.N : 1;
-        const double Lo = tp ? c[0] : 0.0, Li = tp ? c[1] : 0.0, W = tp ? c[2] : 0.0;
-        load_coefs(c + 4, op.M, cr, ci);
+        const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2);
         if (tp) fwd_drift(s, Lo, tangent);
         for (int sl = 0; sl < N; ++sl) {
           if (tape) {
-            double *t = tape + 10 * (kidx++);
-            t[0] = s.x;
-            t[1] = s.y;
+            double *t = a.tape;
+            const int k = kidx++;
+            t[tidx(a, tt, k, 0, nf, j)] = s.x;
+            t[tidx(a, tt, k, 1, nf, j)] = s.y;
             if (tangent)
-              for (int j = 0; j < 4; ++j) {
-                t[2 + j] = s.T[j];
-                t[6 + j] = s.T[8 + j];
+#pragma unroll
+              for (int q = 0; q < 4; ++q) {
+                t[tidx(a, tt, k, 2 + q, nf, j)] = s.T[q];
+                t[tidx(a, tt, k, 6 + q, nf, j)] = s.T[8 + q];
               }
           }
-          fwd_kick(s, cr, ci, op.M, oo, tangent);
+          fwd_kick(s, c + KHDR, op.M, oo, tangent);
           if (tp && W != 0.0) fwd_weak(s, W, tangent);
           if (tp) fwd_drift(s, sl < N - 1 ? Li : Lo, tangent);
         }
@@ -190,6 +204,7 @@ __device__ __forceinline__ void rev_drift(Bar &b, double L, bool tangent) {
   b.px = fma(b.x, L, b.px);
   b.py = fma(b.y, L, b.py);
   if (tangent)
+#pragma unroll
     for (int j = 0; j < 4; ++j) {
       b.T[4 + j] = fma(b.T[j], L, b.T[4 + j]);
       b.T[12 + j] = fma(b.T[8 + j], L, b.T[12 + j]);
@@ -199,90 +214,96 @@ __device__ __forceinline__ void rev_drift(Bar &b, double L, bool tangent) {
 __device__ __forceinline__ void rev_weak(Bar &b, double W, bool tangent) {
   b.x = fma(-W, b.px, b.x);
   if (tangent)
+#pragma unroll
     for (int j = 0; j < 4; ++j) b.T[j] = fma(-W, b.T[4 + j], b.T[j]);
 }
 
-// reverse of one kick at recorded (x, y) [and tangent rows]; returns the
-// cotangent of the op's parameter coefficient (order pm)
-__device__ double rev_kick(Bar &b, const double *t, const double *cr, const double *ci, int M,
-                           double o, bool tangent, int pm) {
-  const double x = t[0], y = t[1];
-  double a1, b1;
-  poly(cr, ci, M, x, y, 1, a1, b1);
+// z^n for small n
+__device__ __forceinline__ void zpow(double x, double y, int n, double &zr, double &zi) {
+  zr = 1.0;
+  zi = 0.0;
+  for (int k = 0; k < n; ++k) {
+    const double tr = fma(zr, x, -zi * y);
+    zi = fma(zr, y, zi * x);
+    zr = tr;
+  }
+}
+
+// reverse of one kick at the taped (x, y) [and tangent rows]; adds the
+// cotangents of the op's parameter coefficient to g0 (S term, weight z^pm) and
+// g1 (S' term, weight z^(pm-1)), both still to be scaled by dK/dk / n!
+__device__ __forceinline__ void rev_kick(Bar &b, const DiffArgs &a, int tt, int k, int j,
+                                         const double *co, int M, double o, bool tangent, int pm,
+                                         double &g0, double &g1) {
+  const int nf = tangent ? 10 : 2;
+  const double x = a.tape[tidx(a, tt, k, 0, nf, j)], y = a.tape[tidx(a, tt, k, 1, nf, j)];
+  double s0r, s0i, a1, b1, a2, b2;
+  if (tangent)
+    series<2>(co, M, x, y, s0r, s0i, a1, b1, a2, b2);
+  else
+    series<1>(co, M, x, y, s0r, s0i, a1, b1, a2, b2);
   a1 *= o;
   b1 *= o;
   // state: px' = px - Re S, py' = py + Im S
-  double xb = -b.px * a1 + b.py * b1;
-  double yb = b.px * b1 + b.py * a1;
-  // parameter (real coefficient of order pm): dS/dc = o z^pm / pm!
-  double gr = 0.0;
-  if (pm >= 0) {
-    double zr = 1.0, zi = 0.0;
-    for (int k = 0; k < pm; ++k) {
-      const double tr = zr * x - zi * y;
-      zi = zr * y + zi * x;
-      zr = tr;
-    }
-    const double w = o / fact(pm);
-    gr = -b.px * zr * w + b.py * zi * w;
+  double xb = fma(-b.px, a1, b.py * b1);
+  double yb = fma(b.px, b1, b.py * a1);
+  if (pm >= 0) {  // dS/dc = o z^pm / pm!
+    double zr, zi;
+    zpow(x, y, pm, zr, zi);
+    g0 += o * fma(-b.px, zr, b.py * zi);
   }
   if (tangent) {
-    double a2 = 0.0, b2 = 0.0;
-    if (M > 2) poly(cr, ci, M, x, y, 2, a2, b2);
-    a2 *= o;
-    b2 *= o;
+    a2 *= 2.0 * o;
+    b2 *= 2.0 * o;
     double Ab = 0.0, Bb = 0.0;
-    for (int j = 0; j < 4; ++j) {
-      const double dx = t[2 + j], dy = t[6 + j];
-      const double pxb = b.T[4 + j], pyb = b.T[12 + j];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const double dx = a.tape[tidx(a, tt, k, 2 + q, nf, j)];
+      const double dy = a.tape[tidx(a, tt, k, 6 + q, nf, j)];
+      const double pxb = b.T[4 + q], pyb = b.T[12 + q];
       // T_px -= a1 dx - b1 dy ; T_py += b1 dx + a1 dy
-      b.T[j] += -pxb * a1 + pyb * b1;
-      b.T[8 + j] += pxb * b1 + pyb * a1;
-      Ab += -pxb * dx + pyb * dy;
-      Bb += pxb * dy + pyb * dx;
+      b.T[q] += fma(-pxb, a1, pyb * b1);
+      b.T[8 + q] += fma(pxb, b1, pyb * a1);
+      Ab += fma(-pxb, dx, pyb * dy);
+      Bb += fma(pxb, dy, pyb * dx);
     }
     // a1 + i b1 = S'(z): d/dx = S'' , d/dy = i S''
-    xb += Ab * a2 + Bb * b2;
-    yb += -Ab * b2 + Bb * a2;
+    xb += fma(Ab, a2, Bb * b2);
+    yb += fma(-Ab, b2, Bb * a2);
     if (pm >= 1) {  // dS'/dc = o z^(pm-1) / (pm-1)!
-      double zr = 1.0, zi = 0.0;
-      for (int k = 0; k < pm - 1; ++k) {
-        const double tr = zr * x - zi * y;
-        zi = zr * y + zi * x;
-        zr = tr;
-      }
-      const double w = o / fact(pm - 1);
-      gr += Ab * zr * w + Bb * zi * w;
+      double zr, zi;
+      zpow(x, y, pm - 1, zr, zi);
+      g1 += o * fma(Ab, zr, Bb * zi);
     }
   }
   b.x += xb;
   b.y += yb;
-  return gr;
 }
 
-// reverse of one turn using its tape; accumulates parameter cotangents
+// reverse of turn `tt` of the segment from its tape; accumulates parameter
+// cotangents
 __device__ void turn_reverse(Bar &b, const DiffArgs &a, const double *T0, double o, bool tangent,
-                             const double *tape, double *pbar) {
+                             int j, int tt) {
   int kidx = a.kicks_per_turn;
-  double cr[MAXC], ci[MAXC];
   for (int i = a.n_ops - 1; i >= 0; --i) {
     const DOp op = a.ops[i];
     const double *c = T0 + op.toff;
     const double oo = op.achro ? 1.0 : o;
     switch (op.kind) {
       case D_DRIFT:
-        rev_drift(b, c[0], tangent);
+        rev_drift(b, __ldg(c), tangent);
         break;
       case D_ALIGN:
         break;  // translation: cotangents unchanged
       case D_EDGE: {
-        const double curv = c[0] * oo;
-        b.x = fma(b.px * curv, c[1], b.x);
-        b.y = fma(-(b.py * curv), c[2], b.y);
+        const double curv = __ldg(c) * oo, e1 = __ldg(c + 1), e2 = __ldg(c + 2);
+        b.x = fma(b.px * curv, e1, b.x);
+        b.y = fma(-(b.py * curv), e2, b.y);
         if (tangent)
-          for (int j = 0; j < 4; ++j) {
-            b.T[j] = fma(b.T[4 + j] * curv, c[1], b.T[j]);
-            b.T[8 + j] = fma(-(b.T[12 + j] * curv), c[2], b.T[8 + j]);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            b.T[q] = fma(b.T[4 + q] * curv, e1, b.T[q]);
+            b.T[8 + q] = fma(-(b.T[12 + q] * curv), e2, b.T[8 + q]);
           }
         break;
       }
@@ -290,18 +311,19 @@ __device__ void turn_reverse(Bar &b, const DiffArgs &a, const double *T0, double
       case D_TEAPOT: {
         const bool tp = op.kind == D_TEAPOT;
         const int N = tp ? op.N : 1;
-        const double Lo = tp ? c[0] : 0.0, Li = tp ? c[1] : 0.0, W = tp ? c[2] : 0.0;
-        const double dKdk = c[3];
-        load_coefs(c + 4, op.M, cr, ci);
-        double g = 0.0;
+        const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2);
+        const int pm = op.pslot >= 0 ? op.pm : -1;
+        double g0 = 0.0, g1 = 0.0;
         for (int sl = N - 1; sl >= 0; --sl) {
           if (tp) rev_drift(b, sl < N - 1 ? Li : Lo, tangent);
           if (tp && W != 0.0) rev_weak(b, W, tangent);
-          const double *t = tape + 10 * (--kidx);
-          g += rev_kick(b, t, cr, ci, op.M, oo, tangent, op.pslot >= 0 ? op.pm : -1);
+          rev_kick(b, a, tt, --kidx, j, c + KHDR, op.M, oo, tangent, pm, g0, g1);
         }
         if (tp) rev_drift(b, Lo, tangent);
-        if (op.pslot >= 0) pbar[op.pslot] += g * dKdk;
+        if (op.pslot >= 0) {
+          double &p = a.pbar[static_cast<int64_t>(op.pslot) * a.n_jobs + j];
+          p = fma(g0, __ldg(c + 3), fma(g1, __ldg(c + 4), p));
+        }
         break;
       }
       default:
@@ -310,16 +332,26 @@ __device__ void turn_reverse(Bar &b, const DiffArgs &a, const double *T0, double
   }
 }
 
-__device__ void load_state(St &s, const double *src, bool tangent) {
-  s.x = src[0]; s.px = src[1]; s.y = src[2]; s.py = src[3];
+__device__ void save_ckpt(const St &s, const DiffArgs &a, int c, int j, bool tangent) {
+  double *d = a.ckpt + static_cast<int64_t>(c) * 20 * a.n_jobs + j;
+  d[0] = s.x;
+  d[a.n_jobs] = s.px;
+  d[2 * a.n_jobs] = s.y;
+  d[3 * a.n_jobs] = s.py;
   if (tangent)
-    for (int k = 0; k < 16; ++k) s.T[k] = src[4 + k];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) d[(4 + k) * static_cast<int64_t>(a.n_jobs)] = s.T[k];
 }
 
-__device__ void save_state(const St &s, double *dst, bool tangent) {
-  dst[0] = s.x; dst[1] = s.px; dst[2] = s.y; dst[3] = s.py;
-  if (tangent)
-    for (int k = 0; k < 16; ++k) dst[4 + k] = s.T[k];
+__device__ void load_ckpt(St &s, const DiffArgs &a, int c, int j, bool tangent) {
+  const double *d = a.ckpt + static_cast<int64_t>(c) * 20 * a.n_jobs + j;
+  s.x = d[0];
+  s.px = d[a.n_jobs];
+  s.y = d[2 * a.n_jobs];
+  s.py = d[3 * a.n_jobs];
+#pragma unroll
+  for (int k = 0; k < 16; ++k)
+    s.T[k] = tangent ? d[(4 + k) * static_cast<int64_t>(a.n_jobs)] : 0.0;
 }
 
 __global__ void diff_forward(DiffArgs a) {
@@ -328,17 +360,20 @@ __global__ void diff_forward(DiffArgs a) {
   const bool tangent = a.tangent;
   St s;
   s.x = a.z0[4 * j]; s.px = a.z0[4 * j + 1]; s.y = a.z0[4 * j + 2]; s.py = a.z0[4 * j + 3];
+#pragma unroll
   for (int k = 0; k < 16; ++k) s.T[k] = (k % 5 == 0) ? 1.0 : 0.0;
   const double o = a.o[j];
   const double *T0 = a.tab + (a.seed ? static_cast<int64_t>(a.seed[j]) : 0) * a.tab_stride;
-  const int nck = a.turns / a.ck + 1;
-  double *ck = a.ckpt ? a.ckpt + static_cast<int64_t>(j) * nck * 20 : nullptr;
+  const bool ck = a.ckpt != nullptr;
   for (int t = 0; t < a.turns; ++t) {
-    if (ck && t % a.ck == 0) save_state(s, ck + 20 * (t / a.ck), tangent);
-    turn_forward(s, a, T0, o, tangent, nullptr);
+    if (ck && t % a.ck == 0) save_ckpt(s, a, t / a.ck, j, tangent);
+    turn_forward(s, a, T0, o, tangent, j, 0, false);
   }
-  if (ck && a.turns % a.ck == 0) save_state(s, ck + 20 * (a.turns / a.ck), tangent);
-  save_state(s, a.zT + 20 * j, tangent);
+  if (ck && a.turns % a.ck == 0) save_ckpt(s, a, a.turns / a.ck, j, tangent);
+  double *d = a.zT + 20 * static_cast<int64_t>(j);
+  d[0] = s.x; d[1] = s.px; d[2] = s.y; d[3] = s.py;
+#pragma unroll
+  for (int k = 0; k < 16; ++k) d[4 + k] = tangent ? s.T[k] : 0.0;
 }
 
 __global__ void diff_reverse(DiffArgs a) {
@@ -347,30 +382,19 @@ __global__ void diff_reverse(DiffArgs a) {
   const bool tangent = a.tangent;
   const double o = a.o[j];
   const double *T0 = a.tab + (a.seed ? static_cast<int64_t>(a.seed[j]) : 0) * a.tab_stride;
-  const int nck = a.turns / a.ck + 1;
-  const double *ck = a.ckpt + static_cast<int64_t>(j) * nck * 20;
-  double *seg = a.seg + static_cast<int64_t>(j) * a.ck * 20;
-  double *tape = a.tape + static_cast<int64_t>(j) * a.kicks_per_turn * 10;
-  double *pbar = a.pbar + static_cast<int64_t>(j) * a.n_params;
-  for (int k = 0; k < a.n_params; ++k) pbar[k] = 0.0;
+  for (int k = 0; k < a.n_params; ++k) a.pbar[static_cast<int64_t>(k) * a.n_jobs + j] = 0.0;
   Bar b;
   b.x = a.zbar[4 * j]; b.px = a.zbar[4 * j + 1]; b.y = a.zbar[4 * j + 2]; b.py = a.zbar[4 * j + 3];
+#pragma unroll
   for (int k = 0; k < 16; ++k) b.T[k] = tangent ? a.Tbar[16 * j + k] : 0.0;
   const int last_seg = (a.turns - 1) / a.ck;
   for (int sg = last_seg; sg >= 0; --sg) {
     const int t0 = sg * a.ck;
     const int t1 = min(a.turns, t0 + a.ck);
     St s;
-    load_state(s, ck + 20 * sg, tangent);
-    for (int t = t0; t < t1; ++t) {  // recover the segment's turn starts
-      save_state(s, seg + 20 * (t - t0), tangent);
-      if (t + 1 < t1) turn_forward(s, a, T0, o, tangent, nullptr);
-    }
-    for (int t = t1 - 1; t >= t0; --t) {
-      load_state(s, seg + 20 * (t - t0), tangent);
-      turn_forward(s, a, T0, o, tangent, tape);  // tape this turn
-      turn_reverse(b, a, T0, o, tangent, tape, pbar);
-    }
+    load_ckpt(s, a, sg, j, tangent);
+    for (int t = t0; t < t1; ++t) turn_forward(s, a, T0, o, tangent, j, t - t0, true);
+    for (int t = t1 - 1; t >= t0; --t) turn_reverse(b, a, T0, o, tangent, j, t - t0);
   }
   a.zbar0[4 * j] = b.x; a.zbar0[4 * j + 1] = b.px; a.zbar0[4 * j + 2] = b.y;
   a.zbar0[4 * j + 3] = b.py;
@@ -382,13 +406,14 @@ __global__ void diff_reverse(DiffArgs a) {
 extern "C" {
 
 // All pointers are device pointers; `ops` int32[n_ops][8] (DOp), `tab` f64.
-// Asynchronous on `stream`.  Returns 0 or a CUDA error code (negative).
+// Asynchronous on `stream`.  Returns 0, -1 (bad arguments) or -2 (launch
+// error).
 int ufo_diff_forward(const int32_t *ops, int n_ops, const double *tab, int64_t tab_stride,
                      const int32_t *seed, int n_params, int kicks_per_turn, int n_jobs,
                      const double *z0, const double *o, int turns, int ck, int tangent,
                      double *ckpt, double *zT, void *stream) {
   if (n_jobs <= 0) return 0;
-  if (!ops || !tab || !z0 || !o || !zT || turns < 0 || ck < 1) return -1;
+  if (!ops || n_ops < 0 || !tab || !z0 || !o || !zT || turns < 0 || ck < 1) return -1;
   ufo_diff::DiffArgs a{};
   a.ops = reinterpret_cast<const ufo_diff::DOp *>(ops);
   a.n_ops = n_ops;
@@ -413,11 +438,11 @@ int ufo_diff_forward(const int32_t *ops, int n_ops, const double *tab, int64_t t
 int ufo_diff_reverse(const int32_t *ops, int n_ops, const double *tab, int64_t tab_stride,
                      const int32_t *seed, int n_params, int kicks_per_turn, int n_jobs,
                      const double *o, int turns, int ck, int tangent, const double *ckpt,
-                     const double *zbar, const double *Tbar, double *seg, double *tape,
-                     double *zbar0, double *pbar, void *stream) {
+                     const double *zbar, const double *Tbar, double *tape, double *zbar0,
+                     double *pbar, void *stream) {
   if (n_jobs <= 0) return 0;
-  if (!ops || !tab || !o || !ckpt || !zbar || !seg || !tape || !zbar0 || !pbar || turns < 1 ||
-      ck < 1 || (tangent && !Tbar))
+  if (!ops || n_ops < 0 || !tab || !o || !ckpt || !zbar || !tape || !zbar0 ||
+      (n_params > 0 && !pbar) || turns < 1 || ck < 1 || (tangent && !Tbar))
     return -1;
   ufo_diff::DiffArgs a{};
   a.ops = reinterpret_cast<const ufo_diff::DOp *>(ops);
@@ -435,7 +460,6 @@ int ufo_diff_reverse(const int32_t *ops, int n_ops, const double *tab, int64_t t
   a.ckpt = const_cast<double *>(ckpt);
   a.zbar = zbar;
   a.Tbar = Tbar;
-  a.seg = seg;
   a.tape = tape;
   a.zbar0 = zbar0;
   a.pbar = pbar;

@@ -271,6 +271,7 @@ struct ufo_ctx {
 
 struct ufo_prog {
   ufo_ctx *ctx;
+  int device;  // copied: destruction must not touch the context
   ufo::Op *ops;
   int n_ops;
   double *table;
@@ -608,6 +609,7 @@ int ufo_prog_create(ufo_ctx *ctx, const int32_t *ops, int n_ops, const double *t
   ufo_prog *p = new (std::nothrow) ufo_prog;
   if (!p) return fail(UFO_E_NOMEM, "host allocation");
   p->ctx = ctx;
+  p->device = ctx->device;
   p->n_ops = n_ops;
   p->stride = stride;
   p->n_seeds = n_seeds;
@@ -649,9 +651,11 @@ int ufo_prog_set_table(ufo_prog *prog, const double *table, int n_seeds) {
 }
 
 void ufo_prog_destroy(ufo_prog *prog) {
+  // may run after the context is gone (any destruction order is allowed), so
+  // only the copied device id is used; cudaFree waits for work in flight
   if (!prog) return;
-  cudaSetDevice(prog->ctx->device);
-  cudaStreamSynchronize(prog->ctx->stream);
+  cudaSetDevice(prog->device);
+  cudaDeviceSynchronize();
   cudaFree(prog->ops);
   cudaFree(prog->table);
   delete prog;
@@ -823,6 +827,7 @@ extern "C" int ufo_track_noalloc(const int32_t *ops, int n_ops, const double *d_
 
 struct ufo_graph {
   ufo_ctx *ctx;
+  int device;  // copied: destruction must not touch the context
   cudaGraph_t graph;
   cudaGraphExec_t exec;
 };
@@ -877,6 +882,7 @@ extern "C" int ufo_graph_create(ufo_ctx *ctx, const ufo_prog *prog, const double
     return fail(UFO_E_NOMEM, "host allocation");
   }
   g->ctx = ctx;
+  g->device = ctx->device;
   g->graph = graph;
   g->exec = exec;
   *out = g;
@@ -894,7 +900,8 @@ extern "C" int ufo_graph_launch(ufo_graph *g, void *stream) {
 
 extern "C" void ufo_graph_destroy(ufo_graph *g) {
   if (!g) return;
-  cudaSetDevice(g->ctx->device);
+  cudaSetDevice(g->device);
+  cudaDeviceSynchronize();
   cudaGraphExecDestroy(g->exec);
   cudaGraphDestroy(g->graph);
   delete g;

@@ -29,7 +29,6 @@ import numpy as np
 from . import compiler as C
 
 D_NOP, D_DRIFT, D_TEAPOT, D_KICK, D_ALIGN, D_EDGE = range(6)
-MAXC = 16
 
 
 def _torch():
@@ -64,22 +63,54 @@ class DiffProgram:
             idx = key if isinstance(key, int) else [j for j, e in enumerate(flat) if e.label == key]
             for j in (idx if isinstance(idx, list) else [idx]):
                 slot[j] = (i, {'k1': 1, 'k2': 2, 'k3': 3}[attr])
-        rows = [self._lower(prog, row, flat, slot) for row in prog.table]
-        ops, kicks = rows[0][0], rows[0][2]
-        self.ops = np.ascontiguousarray(np.array(ops, np.int32).reshape(-1, 8))
-        self.tab = np.ascontiguousarray(np.array([r[1] + [0.0] for r in rows], np.float64))
+        ops, tab, kicks = self._lower(prog, flat, slot)
+        ops, tab = self._trim(np.array(ops, np.int32).reshape(-1, 8), tab)
+        self.ops = np.ascontiguousarray(ops)
+        self.tab = np.ascontiguousarray(tab)
         self.n_seeds = self.tab.shape[0]
         self.tab_stride = self.tab.shape[1]
         self.kicks_per_turn = kicks
         self.n_params = len(parameters)
 
     @staticmethod
-    def _lower(prog, row, flat, slot):
+    def _trim(ops, tab):
+        """Drop trailing multipole orders that are zero in every seed (the
+        reference pads coefficient lists with zeros), keeping the order a
+        parameter scales; the constant table is repacked."""
+        out_ops, cols = [], []
+        for op in ops:
+            kind, off, M, ps, pm = int(op[0]), int(op[2]), int(op[4]), int(op[5]), int(op[6])
+            op = op.copy()
+            op[2] = len(cols)
+            if kind in (D_TEAPOT, D_KICK):
+                hdr = list(range(off, off + 5))
+                a = tab[:, off + 5:off + 5 + M]
+                b = tab[:, off + 5 + M:off + 5 + 2 * M]
+                nz = np.nonzero(np.any(a != 0, axis=0) | np.any(b != 0, axis=0))[0]
+                Mt = max(int(nz.max()) + 1 if len(nz) else 1, pm + 1 if ps >= 0 else 1)
+                op[4] = Mt
+                cols += hdr + list(range(off + 5, off + 5 + Mt)) + \
+                    list(range(off + 5 + M, off + 5 + M + Mt))
+            else:
+                n = {D_DRIFT: 1, D_ALIGN: 2, D_EDGE: 3}.get(kind, 0)
+                cols += list(range(off, off + n))
+            out_ops.append(op)
+        cols.append(tab.shape[1] - 1)
+        return np.array(out_ops, np.int32).reshape(-1, 8), tab[:, cols]
+
+    @staticmethod
+    def _lower(prog, flat, slot):
+        """Opcode list and constant columns for all seed rows of ``prog.table``
+        at once: each constant is an array over the rows (or a scalar)."""
+        T = prog.table
         ops, tab = [], []
         kicks = 0
         for r, elem in zip(prog.ops, prog.op_elem):
             kind, fl, off = int(r[0]), int(r[1]), int(r[2])
-            c = row[off:]
+
+            def c(k, off=off):
+                return T[:, off + k]
+
             achro = 1 if fl & C.F_ACHRO else 0
             if kind in (C.OP_NOP, C.OP_OBSERVE, C.OP_APERTURE):
                 continue
@@ -87,51 +118,49 @@ class DiffProgram:
                 if fl & C.F_EXACT:
                     raise NotImplementedError('exact drifts are not differentiated')
                 form = int(r[3])
-                L = c[0] if form == C.DF_MUL else c[0] * c[1] if form == C.DF_MUL2 else c[3]
+                L = c(0) if form == C.DF_MUL else c(0) * c(1) if form == C.DF_MUL2 else c(3)
                 ops.append([D_DRIFT, 0, len(tab), 0, 0, -1, 0, 0])
                 tab += [L]
             elif kind == C.OP_ALIGN:
                 ops.append([D_ALIGN, 0, len(tab), 0, 0, -1, 0, 0])
-                tab += [c[0] if fl & C.F_AX else 0.0, c[1] if fl & C.F_AY else 0.0]
+                tab += [c(0) if fl & C.F_AX else 0.0, c(1) if fl & C.F_AY else 0.0]
             elif kind == C.OP_EDGE:
                 if fl & C.F_RTPSI:
                     raise NotImplementedError('fringe-field edges with chromatic psi')
                 ops.append([D_EDGE, 0, len(tab), 0, 0, -1, 0, achro])
-                tab += [c[0], c[1] if fl & C.F_T1 else 0.0, c[2] if fl & C.F_T2 else 0.0]
+                tab += [c(0), c(1) if fl & C.F_T1 else 0.0, c(2) if fl & C.F_T2 else 0.0]
             elif kind in (C.OP_TEAPOT, C.OP_KICK):
                 tp = kind == C.OP_TEAPOT
                 if tp:
                     N, nn, ns, mn, ms = (int(v) for v in r[3:8])
                     if fl & C.F_EXACT:
                         raise NotImplementedError('exact drifts are not differentiated')
-                    Lo = c[0]
+                    Lo = c(0)
                     fi = (fl >> C.SH_FINNER) & 3
                     k = 1
                     if N > 1:
-                        Li = c[1] if fi == C.DF_MUL else c[4]
+                        Li = c(1) if fi == C.DF_MUL else c(4)
                         k += 1 if fi == C.DF_MUL else 4
                     else:
                         Li = 0.0
-                    ck = c[k:]
                 else:
                     N = 1
                     nn, ns, mn, ms = (int(v) for v in r[3:7])
                     Lo = Li = 0.0
-                    ck = c
+                    k = 0
                 M = max(nn, ns, 1)
-                if M > MAXC:
-                    raise NotImplementedError(f'more than {MAXC} multipole orders')
-                cr, ci = np.zeros(M), np.zeros(M)
-                q = 0
+                fac = [float(math.factorial(n)) for n in range(M)]
+                cr, ci = [0.0] * M, [0.0] * M
+                q = k
                 for j in range(nn):
                     if mn >> j & 1:
-                        cr[j] = ck[q]
+                        cr[j] = c(q) / fac[j]
                         q += 1
                 for j in range(ns):
                     if ms >> j & 1:
-                        ci[j] = ck[q]
+                        ci[j] = c(q) / fac[j]
                         q += 1
-                W = ck[q] if tp and fl & C.F_WEAK else 0.0
+                W = c(q) if tp and fl & C.F_WEAK else 0.0
                 ps, pm = slot.get(elem, (-1, 0))
                 if pm >= M:  # the coefficient was truncated away (LINEAR): no effect
                     ps = -1
@@ -140,16 +169,23 @@ class DiffProgram:
                     dKdk = (float(e.length) / N) if tp else 1.0
                 else:
                     dKdk = 0.0
+                g0 = dKdk / fac[pm] if ps >= 0 else 0.0
+                g1 = dKdk / fac[pm - 1] if ps >= 0 and pm >= 1 else 0.0
                 ops.append([D_TEAPOT if tp else D_KICK, 0, len(tab), N, M, ps, pm, achro])
-                tab += [Lo, Li, W, dKdk] + list(cr) + list(ci)
+                tab += [Lo, Li, W, g0, g1] + cr + ci
                 kicks += N
             else:
                 raise NotImplementedError(f'{C.OP_NAMES[kind]} elements are not differentiated')
+        S = T.shape[0]
+        tab = np.stack([np.broadcast_to(np.asarray(v, np.float64), (S,)) for v in tab + [0.0]],
+                       axis=1) if tab else np.zeros((S, 1))
         return ops, tab, kicks
 
 
 class DiffEngine:
-    """Device copy of a DiffProgram and the two kernels."""
+    """Device copy of a DiffProgram and the two kernels.  Kernels run on
+    torch's current stream; ``device_ms`` and ``launches`` accumulate their
+    CUDA-event time and count."""
 
     def __init__(self, dprog, device=0):
         torch = _torch()
@@ -160,9 +196,24 @@ class DiffEngine:
         self.p = dprog
         self.ops = torch.from_numpy(dprog.ops).to(self.dev)
         self.tab = torch.from_numpy(dprog.tab).to(self.dev)
+        self.device_ms = 0.0
+        self.launches = 0
 
     def _ptr(self, t):
         return self.capi.ptr(t.data_ptr()) if t is not None else None
+
+    def _run(self, fn, name):
+        torch = _torch()
+        st = torch.cuda.current_stream(self.dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        rc = fn(self.capi.ptr(st.cuda_stream))
+        e1.record(st)
+        if rc:
+            raise RuntimeError(f'{name} failed ({rc})')
+        e1.synchronize()
+        self.device_ms += e0.elapsed_time(e1)
+        self.launches += 1
 
     def forward(self, z0, o, turns, tangent=False, ck=None, seed=None):
         """z0 [J, 4], o [J], seed [J] (constant-table row of each job, default 0)
@@ -180,43 +231,40 @@ class DiffEngine:
             sd = torch.as_tensor(seed, device=self.dev)
         ck = ck or max(1, turns)
         nck = turns // ck + 1
-        ckpt = torch.zeros((J, nck, 20), dtype=torch.float64, device=self.dev)
+        ckpt = torch.zeros((nck, 20, J), dtype=torch.float64, device=self.dev)
         zT = torch.zeros((J, 20), dtype=torch.float64, device=self.dev)
-        rc = self.lib.ufo_diff_forward(
+        self._run(lambda st: self.lib.ufo_diff_forward(
             self._ptr(self.ops), self.ops.shape[0], self._ptr(self.tab), self.p.tab_stride,
             self._ptr(sd), self.p.n_params, self.p.kicks_per_turn, J, self._ptr(z0), self._ptr(o),
-            int(turns), int(ck), int(bool(tangent)), self._ptr(ckpt), self._ptr(zT), None)
-        if rc:
-            raise RuntimeError(f'ufo_diff_forward failed ({rc})')
-        torch.cuda.synchronize(self.dev)
+            int(turns), int(ck), int(bool(tangent)), self._ptr(ckpt), self._ptr(zT), st),
+            'ufo_diff_forward')
         return zT.cpu().numpy(), (ckpt, o, turns, ck, tangent, sd)
 
-    def reverse(self, state, zbar, Tbar=None):
+    def reverse(self, state, zbar, Tbar=None, sum_jobs=False):
         """Cotangents of the final state -> (cotangent of z0 [J, 4],
-        parameter cotangents [J, n_params])."""
+        parameter cotangents [J, n_params], or their sum over jobs [n_params]
+        with ``sum_jobs``)."""
         torch = _torch()
         ckpt, o, turns, ck, tangent, sd = state
-        J = ckpt.shape[0]
+        J = ckpt.shape[2]
         zbar = torch.as_tensor(np.ascontiguousarray(zbar, np.float64), device=self.dev)
         Tb = None
         if tangent:
             Tb = torch.as_tensor(np.ascontiguousarray(Tbar, np.float64).reshape(J, 16),
                                  device=self.dev)
-        seg = torch.empty((J, ck, 20), dtype=torch.float64, device=self.dev)
-        tape = torch.empty((J, max(1, self.p.kicks_per_turn), 10), dtype=torch.float64,
-                           device=self.dev)
+        nf = 10 if tangent else 2
+        tape = torch.empty((min(ck, turns), max(1, self.p.kicks_per_turn), nf, J),
+                           dtype=torch.float64, device=self.dev)
         zbar0 = torch.empty((J, 4), dtype=torch.float64, device=self.dev)
-        pbar = torch.empty((J, max(1, self.p.n_params)), dtype=torch.float64, device=self.dev)
-        rc = self.lib.ufo_diff_reverse(
+        pbar = torch.empty((max(1, self.p.n_params), J), dtype=torch.float64, device=self.dev)
+        self._run(lambda st: self.lib.ufo_diff_reverse(
             self._ptr(self.ops), self.ops.shape[0], self._ptr(self.tab), self.p.tab_stride,
             self._ptr(sd), self.p.n_params, self.p.kicks_per_turn, J, self._ptr(o), int(turns),
-            int(ck), int(bool(tangent)),
-            self._ptr(ckpt), self._ptr(zbar), self._ptr(Tb), self._ptr(seg), self._ptr(tape),
-            self._ptr(zbar0), self._ptr(pbar), None)
-        if rc:
-            raise RuntimeError(f'ufo_diff_reverse failed ({rc})')
-        torch.cuda.synchronize(self.dev)
-        return zbar0.cpu().numpy(), pbar[:, :self.p.n_params].cpu().numpy()
+            int(ck), int(bool(tangent)), self._ptr(ckpt), self._ptr(zbar), self._ptr(Tb),
+            self._ptr(tape), self._ptr(zbar0), self._ptr(pbar), st), 'ufo_diff_reverse')
+        pb = pbar[:self.p.n_params]
+        pb = pb.sum(dim=1) if sum_jobs else pb.T
+        return zbar0.cpu().numpy(), pb.cpu().numpy()
 
 
 # ----------------------------------------------------------------- optics
@@ -269,7 +317,8 @@ def closed_orbits(engine, dps, z0=None, max_iter=30, seed=None):
 
 class OpticsModel:
     """Closed orbit, tunes and chromaticity of a line as functions of the
-    element strengths named in ``parameters``."""
+    element strengths named in ``parameters``; one or many rows of strengths
+    (error seeds) at a time."""
 
     def __init__(self, line, flags, parameters, h_dp=1e-5, device=0):
         self.line = line
@@ -282,18 +331,10 @@ class OpticsModel:
         return DiffEngine(DiffProgram(self.line, self.flags, self.parameters, values),
                           self.device)
 
-    def evaluate(self, values):
-        eng = self.engine(values)
-        dps = [0.0, self.h, -self.h]
-        z, J, res = closed_orbits(eng, dps)
-        q = np.array([[tune_and_grad(J[i], p)[0] for p in (0, 1)] for i in range(3)])
-        xi = (q[1] - q[2]) / (2 * self.h)
-        out = np.concatenate([z[0], q[0], xi])
-        return out, (eng, z, J, dps)
-
-    def evaluate_many(self, values):
-        """evaluate() for S rows of parameter values in one batch of launches
-        (the S x 3 closed-orbit problems run as one job list).  -> out [S, 8]."""
+    def evaluate_batch(self, values):
+        """values [S, P] -> (out [S, 8], saved).  The S x 3 closed-orbit problems
+        (dp = 0, +h, -h per row) run as one job list; each job stops on its own,
+        so a row's result does not depend on the other rows."""
         values = np.atleast_2d(np.asarray(values, np.float64))
         S = values.shape[0]
         eng = self.engine(values)
@@ -303,36 +344,58 @@ class OpticsModel:
         q = np.array([[tune_and_grad(J[i], p)[0] for p in (0, 1)] for i in range(3 * S)])
         q = q.reshape(S, 3, 2)
         xi = (q[:, 1] - q[:, 2]) / (2 * self.h)
-        return np.concatenate([z.reshape(S, 3, 4)[:, 0], q[:, 0], xi], axis=1)
+        out = np.concatenate([z.reshape(S, 3, 4)[:, 0], q[:, 0], xi], axis=1)
+        return out, (eng, z, J, dps, seed, S)
+
+    def evaluate(self, values):
+        """One row of strengths -> (out [8], saved)."""
+        out, saved = self.evaluate_batch(np.asarray(values, np.float64).reshape(1, -1))
+        return out[0], saved
+
+    def evaluate_many(self, values):
+        return self.evaluate_batch(values)[0]
 
     def vjp(self, saved, gbar):
-        """Vector-Jacobian product of evaluate() for the 8 output cotangents."""
-        eng, z, J, dps = saved
-        gbar = np.asarray(gbar, np.float64)
-        zco_bar = gbar[:4]
-        qbar = gbar[4:6]
-        xibar = gbar[6:8]
-        Mbar = np.zeros((3, 4, 4))
-        for i, w in ((0, 1.0), (1, 1.0 / (2 * self.h)), (2, -1.0 / (2 * self.h))):
-            for p in (0, 1):
-                coeff = (qbar[p] if i == 0 else 0.0) + (xibar[p] * w if i else 0.0)
-                if coeff == 0.0:
-                    continue
-                _, dq = tune_and_grad(J[i], p)
-                a = 0 if p == 0 else 2
-                Mbar[i, a, a] += coeff * dq
-                Mbar[i, a + 1, a + 1] += coeff * dq
-        o = 1.0 / (np.asarray(dps) + 1.0)
+        """Vector-Jacobian products of evaluate_batch().  ``gbar`` holds output
+        cotangents [8] (one row), [S, 8] or [S, R, 8] (R cotangent vectors per
+        row, e.g. R = 8 unit vectors for the whole Jacobian); the result has the
+        same leading shape with P parameter cotangents.  All S x R x 3 jobs run
+        in one tangent-adjoint and one plain-adjoint launch pair."""
+        eng, z, J, dps, seed, S = saved
+        g = np.asarray(gbar, np.float64)
+        lead = g.shape[:-1]
+        G = g.reshape(S, -1, 8)
+        R = G.shape[1]
+        # xi = (Q(+h) - Q(-h)) / 2h: weights of the xi cotangent per dp job
+        w = np.array([0.0, 1.0 / (2 * self.h), -1.0 / (2 * self.h)])
+        # dQ/dc for every (row, dp) and plane
+        dq = np.array([[tune_and_grad(J[i], p)[1] for p in (0, 1)] for i in range(3 * S)])
+        dq = dq.reshape(S, 1, 3, 2)
+        coeff = G[:, :, None, 6:8] * w[None, None, :, None]           # [S, R, 3, 2]
+        coeff[:, :, 0] += G[:, :, 4:6]
+        coeff = coeff * dq
+        Mbar = np.zeros((S, R, 3, 4, 4))
+        for p, a in ((0, 0), (1, 2)):
+            Mbar[..., a, a] += coeff[..., p]
+            Mbar[..., a + 1, a + 1] += coeff[..., p]
+        jobs = (np.arange(S)[:, None, None] * 3 + np.arange(3)[None, None, :]) + \
+            np.zeros((1, R, 1), np.int64)                                # [S, R, 3]
+        jobs = jobs.reshape(-1)
+        zj, Jj, sj = z[jobs], J[jobs], seed[jobs]
+        o = 1.0 / (dps[jobs] + 1.0)
         # (1) adjoint of the tangent-augmented one-turn map at fixed z*
-        _, st = eng.forward(z, o, 1, tangent=True)
-        v, ka = eng.reverse(st, np.zeros((3, 4)), Mbar.reshape(3, 16))
+        _, st = eng.forward(zj, o, 1, tangent=True, seed=sj)
+        v, ka = eng.reverse(st, np.zeros((len(jobs), 4)), Mbar.reshape(-1, 16))
         # (2) implicit differentiation of F(z*) = z*: lambda = (I - J)^-T (zbar + v)
-        zb = v.copy()
-        zb[0] += zco_bar
-        lam = np.linalg.solve(np.transpose(np.eye(4)[None] - J, (0, 2, 1)), zb[:, :, None])[:, :, 0]
-        _, st = eng.forward(z, o, 1, tangent=False)
+        zb = v.reshape(S, R, 3, 4).copy()
+        zb[:, :, 0] += G[:, :, :4]
+        zb = zb.reshape(-1, 4)
+        lam = np.linalg.solve(np.transpose(np.eye(4)[None] - Jj, (0, 2, 1)),
+                              zb[:, :, None])[:, :, 0]
+        _, st = eng.forward(zj, o, 1, tangent=False, seed=sj)
         _, kb = eng.reverse(st, lam)
-        return (ka + kb).sum(axis=0)
+        kbar = (ka + kb).reshape(S, R, 3, -1).sum(axis=2)
+        return kbar.reshape(*lead, -1)
 
 
 def _function_classes():
@@ -374,8 +437,8 @@ def _function_classes():
             zbar = np.zeros((zT.shape[0], 4))
             zbar[:, 0] = 2 * zT[:, 0] * g
             zbar[:, 2] = 2 * zT[:, 2] * g
-            _, pbar = ctx.eng.reverse(ctx.st, zbar)
-            return torch.as_tensor(pbar.sum(axis=0), dtype=torch.float64), None, None, None, None
+            _, pbar = ctx.eng.reverse(ctx.st, zbar, sum_jobs=True)
+            return torch.as_tensor(pbar, dtype=torch.float64), None, None, None, None
 
     return OpticsFunction, AmplitudeFunction
 
