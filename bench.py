@@ -47,11 +47,13 @@ def parse():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--mode', default='fma', choices=['strict', 'fma'])
     ap.add_argument('--no-alt', action='store_true', help='skip the other-mode measurement')
+    ap.add_argument('--no-yoshida', action='store_true',
+                    help='skip the Yoshida-4 measurement of the C2 ring')
     ap.add_argument('--turns-per-step', type=int, default=1000)
     ap.add_argument('--particles', type=int, default=65536)
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
-    ap.add_argument('--workload', default='c2', choices=['c2', 'c4', 'c5'])
+    ap.add_argument('--workload', default='c2', choices=['c2', 'c3', 'c4', 'c5'])
     ap.add_argument('--seeds', type=int, default=64, help='C4: number of seeds')
     ap.add_argument('--turn-div', type=int, default=4, help='C4: divide turn counts by this')
     ap.add_argument('--c5-seeds', type=int, default=256,
@@ -228,10 +230,10 @@ def bench_ours(args):
             import torch.distributed as tdist
             tdist.barrier()
 
-    def timed_device(mode, steps, warmup):
+    def timed_device(mode, steps, warmup, yoshida=False):
         """Exactly `steps` chained launches (1000 turns each) on HBM-resident
         coordinates, L2 flushed between launches; CUDA events on the stream."""
-        flags = u.KICK | (u.FMA if mode == 'fma' else 0)
+        flags = u.KICK | (u.FMA if mode == 'fma' else 0) | (u.YOSHIDA if yoshida else 0)
         tflags = capi.UFO_TRACK_FMA if mode == 'fma' else 0
         prog = C.compile_line(ring, flags, where=[-1])
         dprog = capi.DeviceProgram(ctx, prog)
@@ -283,6 +285,7 @@ def bench_ours(args):
     peak = ctypes_peak(ctx)
     other = 'strict' if args.mode == 'fma' else 'fma'
     alt = None if args.no_alt else timed_device(other, min(3, args.steps), 1)
+    ysh = None if args.no_yoshida else timed_device(args.mode, min(2, args.steps), 1, True)
 
     e2e = None
     if not args.no_e2e:
@@ -336,6 +339,14 @@ def bench_ours(args):
                        'flops_per_particle_turn': alt['flops_per_particle_turn'],
                        'note': ('bit-identical to the reference' if other == 'strict' else
                                 'fused multiply-add, within 1e-9 of strict after 1000 turns')}
+    if ysh:
+        line['yoshida4'] = {
+            'value': ysh['value'], 'ms_per_step': ysh['ms_per_step'], 'steps': min(2, args.steps),
+            'roofline_frac': ysh['achieved'] / peak if peak else None,
+            'flops_per_particle_turn': ysh['flops_per_particle_turn'], 'mode': args.mode,
+            'note': 'the C2 configuration as specified (4th-order Yoshida, 4 slices); the '
+                    'reference has only TEAPOT, so the headline and the reference arm use '
+                    'TEAPOT'}
     if e2e:
         line['e2e'] = e2e
     if cb:
@@ -401,6 +412,110 @@ def bench_c4(args):
             'plain_one_launch_per_seed': {'value': pet / (ms_plain / 1e3), 'ms': ms_plain},
             'speedup_batched_vs_plain': ms_plain / ms_batch,
             'identical_results': identical, 'gpu_launches': launches}
+    print(json.dumps(line), flush=True)
+
+
+def bench_c3(args):
+    """Dynamic-aperture scan (C3): 256 x 256 polar grid x 3 momenta = 196,608
+    particles, 2,048 turns, StableAperture loss test, on the C1 ring with a 10 mm
+    aperture and C4-style errors (survival very uneven).  The persistent kernel
+    (lanes refilled from a work counter at turn boundaries) against the plain
+    one-thread-per-particle kernel; loss turns must be identical.  Throughput
+    counts the particle-turns actually tracked (a lost particle stops)."""
+    import torch
+    import ufo_gb300 as u
+    from ufo_gb300 import capi, compiler as C, workloads as W
+    torch.cuda.set_device(0)
+    dev = torch.device('cuda', 0)
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    ctx = u.context(0)
+    lib = capi.load()
+    ring = W.c3_ring(u)
+    n_elem = len(ring.flatten())
+    grid = W.c3_grid()
+    n, T = grid.shape[0], 2048
+    flags = u.KICK | (u.FMA if args.mode == 'fma' else 0)
+    tflags = capi.UFO_TRACK_FMA if args.mode == 'fma' else 0
+    prog = C.compile_line(ring, flags, where=[-1])
+    dprog = capi.DeviceProgram(ctx, prog)
+    perm = np.random.default_rng(3).permutation(n)
+    inputs = {'sorted': torch.from_numpy(grid).to(dev),
+              'shuffled': torch.from_numpy(np.ascontiguousarray(grid[perm])).to(dev)}
+    lost = torch.empty(n, dtype=torch.int32, device=dev)
+    final = torch.empty((n, 6), dtype=torch.float64, device=dev)
+
+    def launch(coords, plain):
+        capi.check(lib.ufo_track_device(
+            ctx.handle, dprog.handle, capi.ptr(coords.data_ptr()), None, None, n, T,
+            capi.UFO_MODE_SA, tflags | (capi.UFO_TRACK_PLAIN if plain else 0), 0, 1, None,
+            capi.ptr(lost.data_ptr()), capi.ptr(final.data_ptr()), capi.ptr(stream.cuda_stream)))
+
+    def timed(order, plain, steps):
+        coords = inputs[order]
+        for _ in range(args.warmup):
+            launch(coords, plain)
+        torch.cuda.synchronize()
+        l0 = ctx.launches()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            launch(coords, plain)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        lo = lost.cpu().numpy().view(np.uint32).astype(np.int64)
+        if order == 'shuffled':
+            un = np.empty_like(lo)
+            un[perm] = lo
+            lo = un
+        return e0.elapsed_time(e1) / steps, ctx.launches() - l0, lo
+
+    clocks = Clocks(0)
+    clocks.start()
+    runs = {}
+    for order in ('sorted', 'shuffled'):
+        for plain in (False, True):
+            runs[(order, plain)] = timed(order, plain, args.steps if not plain else
+                                         max(1, args.steps // 2))
+    ms_p, launches, lost_p = runs[('sorted', False)]
+    ms_plain, _, lost_plain = runs[('sorted', True)]
+    clk = clocks.stop()
+    peak = ctypes_peak(ctx)
+    # a particle lost at the end of turn t tracked t + 1 turns
+    tracked = np.where(lost_p < T, lost_p + 1, T).sum()
+    pet = float(tracked) * n_elem
+    fl = prog.flops_fast if args.mode == 'fma' else prog.flops
+    surv = float(np.mean(lost_p >= T))
+    line = {'metric': 'FP64 particle*element*turns/s', 'value': pet / (ms_p / 1e3),
+            'unit': 'particle*element*turns/s', 'n_gpus': 1, 'steps': args.steps,
+            'warmup': args.warmup, 'ms_per_step': ms_p, 'higher_is_better': True,
+            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
+            'config': {'workload': 'C3 dynamic aperture: 256x256 polar grid (r 0-25 mm, '
+                                   'angle 0-pi/2) x dp {-2%, 0, +2%}, 2048 turns, SA loss '
+                                   'test, C1 ring with 10 mm apertures and C4 seed-0 errors',
+                       'particles': n, 'turns': T, 'elements': n_elem, 'mode': args.mode,
+                       'l2': 'inputs resident; each launch re-reads 9.4 MB of coordinates'},
+            'roofline': {'bound': 'fp64', 'achieved': fl * tracked / (ms_p / 1e3) / 1e9,
+                         'peak': peak, 'unit': 'GFLOP/s',
+                         'frac': fl * tracked / (ms_p / 1e3) / 1e9 / peak if peak else None,
+                         'traffic': None, 'flops_per_particle_turn': fl,
+                         'peak_source': 'measured live: ufo_fp64_peak'},
+            'survival_fraction': surv,
+            'particle_turns_tracked': int(tracked),
+            'plain_one_thread_per_particle': {'value': pet / (ms_plain / 1e3), 'ms': ms_plain},
+            'speedup_persistent_vs_plain': ms_plain / ms_p,
+            'shuffled_order': {
+                'persistent': pet / (runs[('shuffled', False)][0] / 1e3),
+                'plain': pet / (runs[('shuffled', True)][0] / 1e3),
+                'speedup_persistent_vs_plain':
+                    runs[('shuffled', True)][0] / runs[('shuffled', False)][0],
+                'note': 'the same grid in a seeded random order: warps of the plain '
+                        'kernel mix survivors and early losses'},
+            'identical_loss_turns': bool(all(np.array_equal(lost_p, r[2])
+                                             for r in runs.values())),
+            'gpu_launches': launches}
+    if clk:
+        line['clocks'] = clk
     print(json.dumps(line), flush=True)
 
 
@@ -611,6 +726,8 @@ def main():
     args = parse()
     if args.impl == 'reference':
         bench_reference(args)
+    elif args.workload == 'c3':
+        bench_c3(args)
     elif args.workload == 'c4':
         bench_c4(args)
     elif args.workload == 'c5':

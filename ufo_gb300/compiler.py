@@ -361,7 +361,9 @@ class _Lowerer:
 
         fl = F_ACHRO if self.flags & ACHROMATIC else 0
         if self.flags & YOSHIDA:
-            raise NotImplementedError('YOSHIDA integration is not available in this build')
+            if self.flags & EXACT:
+                raise NotImplementedError('YOSHIDA integration with EXACT drifts')
+            return self._yoshida(Lf, slices, ks, weak, elem)
         exact = bool(self.flags & EXACT)
         if exact:
             fl |= F_EXACT
@@ -394,9 +396,6 @@ class _Lowerer:
         Yoshida drift-kick composition (3 kicks of weights d_i/N, 4 drifts of
         c_i*L/N).  No reference counterpart."""
         fl = F_YOSHIDA | (F_ACHRO if self.flags & ACHROMATIC else 0)
-        if self.flags & EXACT:
-            fl |= F_EXACT
-        n = len(ks.norm)
         # kick coefficients scaled per slice are (k*L*f)/N; Yoshida weights
         # multiply them, drifts are c_i * (L*f)/N
         nn, nsk, mn, ms, kconsts = ks.packed()
@@ -411,7 +410,18 @@ class _Lowerer:
             wc = []
         op = Op(OP_TEAPOT, fl, ints=[slices, nn, nsk, mn, ms],
                 consts=drifts + wts + kconsts + wc, elem=elem)
-        op.flops = op.flops_fast = slices * (4 * 4 + 3 * (ks.flops() + 2 + (2 if wc else 0)))
+        # executed arithmetic (no reference expression to follow): the kernel
+        # forms the weighted strengths once per element (quadrupole: K*o*w_i,
+        # sextupole: K*o*0.5*w_i, weak: W*w_i); per slice 4 drifts (4 flops
+        # each) and 3 kicks: quadrupole 4, sextupole 10, general Horner + 4
+        # (weighted accumulation), plus 2 per weak term
+        pat = 0 if nsk else 1 if (nn == 2 and mn == 2) else 2 if (nn == 3 and mn == 4) else \
+            3 if mn == 0 else 0
+        achro = bool(self.flags & ACHROMATIC)
+        per_elem = {0: 0, 1: 3 + (0 if achro else 1), 2: 4 + (0 if achro else 1), 3: 0}[pat] + \
+            (3 if wc else 0)
+        kick = {0: ks.flops() + 4, 1: 4, 2: 10, 3: 0}[pat]
+        op.flops = op.flops_fast = per_elem + slices * (16 + 3 * (kick + (2 if wc else 0)))
         self.emit(op)
 
     def edge(self, length, angle, e, fringe, elem):

@@ -460,6 +460,84 @@ UFO_DEV void teapot_v(State &s, const Op &op, const double *c) {
   drift_L<FMA>(s, Lo);
 }
 
+// ---------------------------------------------------------------- Yoshida
+// The build's 4th-order integrator (H. Yoshida, Phys. Lett. A 150 (1990) 262;
+// no reference counterpart): each of the N slices of length h = L*f/N is
+//   drift c0 h, kick w0, drift c1 h, kick w1, drift c2 h, kick w2, drift c3 h
+// with c = (w1/2, (w0+w1)/2, (w0+w1)/2, w1/2), w = (w1, w0, w1),
+// w1 = 1/(2 - 2^(1/3)), w0 = 1 - 2 w1.  A kick of weight w applies w times the
+// slice's teapot kick (coefficients (k*L*f)/N) and w times its weak focusing.
+// Table: [c0 h, c1 h, c2 h, c3 h][w0, w1, w2][kick][W].  The weighted kick
+// strengths of the quadrupole/sextupole patterns are formed once per element.
+template <bool FMA, int PAT, bool WEAK>
+UFO_DEV void y_kick(State &s, int nn, int ns, uint32_t mn, uint32_t ms, const double *ck,
+                    bool achro, double w, double t, double Ww) {
+  if (PAT == 0) {
+    // unweighted kick from zero momenta: r = (-dpx, +dpy)
+    const PxPy r = kick_ool<FMA>(s.x, s.y, 0.0, 0.0, s.o, s.bad_o, nn, ns, mn, ms, ck, achro,
+                                 false);
+    if (FMA) {
+      s.px = fma_(w, r.px, s.px);
+      s.py = fma_(w, r.py, s.py);
+    } else {
+      s.px = add(s.px, mul(w, r.px));
+      s.py = add(s.py, mul(w, r.py));
+    }
+  } else if (PAT == 1) {
+    if (FMA) {
+      s.px = fma_(-t, s.x, s.px);
+      s.py = fma_(t, s.y, s.py);
+    } else {
+      s.px = sub(s.px, mul(t, s.x));
+      s.py = add(s.py, mul(t, s.y));
+    }
+  } else if (PAT == 2) {
+    const double a = mul(t, s.x), b = mul(t, s.y);
+    if (FMA) {
+      s.px = fma_(b, s.y, fma_(-a, s.x, s.px));
+      s.py = fma_(b, s.x, fma_(a, s.y, s.py));
+    } else {
+      s.px = sub(s.px, sub(mul(a, s.x), mul(b, s.y)));
+      s.py = add(s.py, add(mul(a, s.y), mul(b, s.x)));
+    }
+  }
+  if (WEAK) s.px = FMA ? fma_(-s.x, Ww, s.px) : sub(s.px, mul(s.x, Ww));
+}
+
+template <bool FMA, int PAT, bool WEAK>
+UFO_DEV void yoshida_v(State &s, const Op &op, const double *c) {
+  const int N = op.i0, nn = op.i1, ns = op.i2;
+  const uint32_t mn = static_cast<uint32_t>(op.i3), ms = static_cast<uint32_t>(op.i4);
+  const bool achro = op.flags & F_ACHRO;
+  const double d0 = ld(c), d1 = ld(c + 1), d2 = ld(c + 2), d3 = ld(c + 3);
+  const double w0 = ld(c + 4), w1 = ld(c + 5), w2 = ld(c + 6);
+  const double *ck = c + 7;
+  double t0 = 0.0, t1 = 0.0, t2 = 0.0, W0 = 0.0, W1 = 0.0, W2 = 0.0;
+  if (PAT == 1 || PAT == 2) {
+    const double o1 = achro ? 1.0 : s.o;
+    double t = mul(ld(ck), o1);
+    if (PAT == 2) t = mul(t, 0.5);
+    t0 = mul(t, w0);
+    t1 = mul(t, w1);
+    t2 = mul(t, w2);
+  }
+  if (WEAK) {
+    const double W = ld(ck + __popc(mn) + __popc(ms));
+    W0 = mul(W, w0);
+    W1 = mul(W, w1);
+    W2 = mul(W, w2);
+  }
+  for (int sl = 0; sl < N; ++sl) {
+    drift_L<FMA>(s, d0);
+    y_kick<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, w0, t0, W0);
+    drift_L<FMA>(s, d1);
+    y_kick<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, w1, t1, W1);
+    drift_L<FMA>(s, d2);
+    y_kick<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, w2, t2, W2);
+    drift_L<FMA>(s, d3);
+  }
+}
+
 // exact-Hamiltonian teapot (rare): generic, out of line
 template <bool FMA>
 __device__ __noinline__ P4 teapot_exact_ool(double x, double px, double y, double py,
@@ -477,6 +555,19 @@ UFO_DEV void teapot(State &s, const Op &op, const double *c) {
   const uint32_t mn = static_cast<uint32_t>(op.i3);
   const int pat = ns != 0 ? 0 : (nn == 2 && mn == 2u) ? 1 : (nn == 3 && mn == 4u) ? 2
                  : mn == 0u ? 3 : 0;
+  if (op.flags & F_YOSHIDA) {
+    switch (pat | ((op.flags & F_WEAK) ? 4 : 0)) {
+      case 0: yoshida_v<FMA, 0, false>(s, op, c); break;
+      case 1: yoshida_v<FMA, 1, false>(s, op, c); break;
+      case 2: yoshida_v<FMA, 2, false>(s, op, c); break;
+      case 3: yoshida_v<FMA, 3, false>(s, op, c); break;
+      case 4: yoshida_v<FMA, 0, true>(s, op, c); break;
+      case 5: yoshida_v<FMA, 1, true>(s, op, c); break;
+      case 6: yoshida_v<FMA, 2, true>(s, op, c); break;
+      default: yoshida_v<FMA, 3, true>(s, op, c); break;
+    }
+    return;
+  }
   const int fi = (op.flags >> SH_FINNER) & 3;
   const int v = pat | (fi == DF_DIV ? 4 : 0) | ((op.flags & F_WEAK) ? 8 : 0);
   switch (v) {

@@ -344,7 +344,10 @@ int64_t op_consts(const int32_t *w) {
       if (!mask_fits(w[3], w[5]) || !mask_fits(w[4], w[6])) return -1;
       return popc32(w[5]) + popc32(w[6]);
     case ufo::OP_TEAPOT: {
-      if (flags & ufo::F_YOSHIDA) return -1;
+      if (flags & ufo::F_YOSHIDA) {  // [4 drifts][3 weights][kick][W]
+        if (exact || w[3] < 1 || !mask_fits(w[4], w[6]) || !mask_fits(w[5], w[7])) return -1;
+        return 7 + popc32(w[6]) + popc32(w[7]) + ((flags & ufo::F_WEAK) ? 1 : 0);
+      }
       if (w[3] < 1 || !mask_fits(w[4], w[6]) || !mask_fits(w[5], w[7])) return -1;
       const int fo = (flags >> ufo::SH_FOUTER) & 3, fi = (flags >> ufo::SH_FINNER) & 3;
       const int co = drift_consts(fo, exact), ci = w[3] > 1 ? drift_consts(fi, exact) : 0;

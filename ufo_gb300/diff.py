@@ -130,6 +130,8 @@ class DiffProgram:
                 ops.append([D_EDGE, 0, len(tab), 0, 0, -1, 0, achro])
                 tab += [c(0), c(1) if fl & C.F_T1 else 0.0, c(2) if fl & C.F_T2 else 0.0]
             elif kind in (C.OP_TEAPOT, C.OP_KICK):
+                if fl & C.F_YOSHIDA:
+                    raise NotImplementedError('Yoshida elements are not differentiated')
                 tp = kind == C.OP_TEAPOT
                 if tp:
                     N, nn, ns, mn, ms = (int(v) for v in r[3:8])
