@@ -134,6 +134,39 @@ def test_full_size_c2_fma_within_tolerance_of_strict():
     assert np.array_equal(fs[idx], ref['final'], equal_nan=True)
 
 
+@pytest.mark.parametrize('which', ['c3', 'c5'])
+def test_general_kicks_fma_within_tolerance_of_strict(which):
+    """General multipole kicks (normal and skew errors of orders 3-6 on every
+    magnet, misalignments): the FMA mode's single complex Horner pass against
+    the strict mode (the reference's two real passes, bit-identical to it):
+    <= 1e-12 relative after 1 turn and 1e-12 * turns after 1000 turns on every
+    regular particle (strict re-tracking from a start perturbed by 1e-15 moves
+    it by less than a tenth of the tolerance)."""
+    import ufo_gb300 as u
+    from ufo_gb300 import capi, compiler as C, workloads as W
+    if which == 'c3':
+        ring, beam = W.c3_ring(u), W.c1_beam(2048, seed=9)
+    else:
+        ring, beam = W.c5_ring(u), W.c2_beam(2048, seed=9)
+    ctx = u.context(0)
+    ps = capi.DeviceProgram(ctx, C.compile_line(ring, u.KICK, where=[-1]))
+    pf = capi.DeviceProgram(ctx, C.compile_line(ring, u.KICK | u.FMA, where=[-1]))
+    for turns in (1, 1000):
+        tol = 1e-12 * turns
+        _, ls, fs = capi.track(ctx, ps, beam, turns, capi.UFO_MODE_TRACK, 0, slots=0)
+        _, _, fp = capi.track(ctx, ps, beam * (1 + 1e-15), turns, capi.UFO_MODE_TRACK, 0,
+                              slots=0)
+        _, lf, ff = capi.track(ctx, pf, beam, turns, capi.UFO_MODE_TRACK, capi.UFO_TRACK_FMA,
+                               slots=0)
+        scale = np.nanmax(np.abs(fs[:, :4]), axis=0)
+        pert = np.max(np.abs(fp[:, :4] - fs[:, :4]) / scale, axis=1)
+        reg = (pert <= tol / 10) & np.all(np.isfinite(fs[:, :4]), axis=1)
+        assert reg.sum() >= 0.9 * len(beam), reg.sum()
+        err = np.max(np.abs(ff[reg, :4] - fs[reg, :4]) / scale)
+        assert err <= tol, (turns, err)
+        assert np.array_equal(ls[reg], lf[reg])
+
+
 def test_seed_batch_equals_individual_launches():
     """One launch over many error seeds == one launch per seed, bit for bit."""
     import ufo_gb300 as u

@@ -122,7 +122,9 @@ class TrackBatch:
         self._graph = g
 
     def launch(self, stream=None, graph=True):
-        """Enqueue the batched launch (graph replay, or a direct launch)."""
+        """Enqueue the batched launch (graph replay, or a direct launch) on
+        the CUDA stream handle ``stream`` (None or 0: the context's own
+        stream, which does not synchronise with the legacy default stream)."""
         if self._dev is None:
             self.upload()
         lib = capi.load()
@@ -230,20 +232,24 @@ def autotune(batch, warps=(8, 12, 16), orders=('lpt', 'seed'), scale=16, use_cac
         saved = batch.pturns
         batch.pturns = np.maximum(1, saved // scale).astype(np.int32)
         times = {}
+        # launches and their events on one stream of our own (the library
+        # launches on the stream it is given)
+        stream = torch.cuda.Stream(torch.device('cuda', batch.ctx.device))
         try:
-            for order in orders:
-                batch.upload(order)
-                for w in warps:
-                    capi.check(capi.load().ufo_ctx_set_tuning(batch.ctx.handle, int(w)))
-                    batch.launch(graph=False)  # warm
-                    torch.cuda.synchronize()
-                    e0 = torch.cuda.Event(enable_timing=True)
-                    e1 = torch.cuda.Event(enable_timing=True)
-                    e0.record()
-                    batch.launch(graph=False)
-                    e1.record()
-                    torch.cuda.synchronize()
-                    times[f'{order}/{w}'] = e0.elapsed_time(e1)
+            with torch.cuda.stream(stream):
+                for order in orders:
+                    batch.upload(order)
+                    for w in warps:
+                        capi.check(capi.load().ufo_ctx_set_tuning(batch.ctx.handle, int(w)))
+                        batch.launch(stream=stream.cuda_stream, graph=False)  # warm
+                        stream.synchronize()
+                        e0 = torch.cuda.Event(enable_timing=True)
+                        e1 = torch.cuda.Event(enable_timing=True)
+                        e0.record(stream)
+                        batch.launch(stream=stream.cuda_stream, graph=False)
+                        e1.record(stream)
+                        stream.synchronize()
+                        times[f'{order}/{w}'] = e0.elapsed_time(e1)
         finally:
             batch.pturns = saved
             batch._dev = None

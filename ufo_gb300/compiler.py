@@ -209,7 +209,23 @@ class KickSpec:
             total += _horner_flops(lst, self.achro, skew)
         return total
 
+    def general(self):
+        """True when the kernels take the general path (not the quadrupole or
+        sextupole short forms, not an empty kick)."""
+        nn, ns, mn, ms, _ = self.packed()
+        if ms:
+            return True
+        return not ((nn == 2 and mn == 2) or (nn == 3 and mn == 4) or mn == 0)
+
     def flops_fast(self):
+        """FMA-mode operations per kick.  General kicks are one complex Horner
+        pass over power-series coefficients: per order below the top 2
+        coefficient scalings + 4 FMA (10 flops), 2 scalings for the top
+        coefficient, the strength factor and 2 FMA for the update."""
+        if self.general():
+            _, _, mn, ms, _ = self.packed()
+            top = (mn | ms).bit_length() - 1
+            return 10 * top + 2 + (0 if self.achro else 1) + 4
         total = 0
         for lst, skew in ((self.norm, False), (self.skew, True)):
             total += _horner_flops(lst, self.achro, skew, fast=True)

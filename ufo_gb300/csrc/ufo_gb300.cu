@@ -311,6 +311,13 @@ int ensure_constants(int device) {
   r[0] = 0.0;
   for (int k = 1; k <= 32; ++k) r[k] = 1.0 / static_cast<double>(k);
   UFO_CUDA(cudaMemcpyToSymbol(ufo::c_rcp_order, r, sizeof r));
+  double rf[33];
+  double fact = 1.0;  // n! is exact in FP64 for n <= 22; above, one rounding per step
+  for (int k = 0; k <= 32; ++k) {
+    if (k > 0) fact *= static_cast<double>(k);
+    rf[k] = 1.0 / fact;
+  }
+  UFO_CUDA(cudaMemcpyToSymbol(ufo::c_rcp_fact, rf, sizeof rf));
   g_const_ready[device] = true;
   return UFO_OK;
 }
