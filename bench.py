@@ -60,6 +60,8 @@ def parse():
                     help='C5: error seeds in the GPU-filling adjoint batch')
     ap.add_argument('--c5-fd-params', type=int, default=8,
                     help='C5: parameters in the sampled multi-turn FD')
+    ap.add_argument('--c5-skip-multiturn', action='store_true',
+                    help='C5: optics gradients only (for profiling captures)')
     return ap.parse_args()
 
 
@@ -392,14 +394,23 @@ def bench_c4(args):
     b.capture()
     for _ in range(args.warmup):
         b.launch(stream=stream.cuda_stream)
+    clocks = Clocks(0)
+    clocks.start()
     l0 = ctx.launches()
     ms_batch = timed(lambda: b.launch(stream=stream.cuda_stream), args.steps)
     launches = ctx.launches() - l0
+    clk = clocks.stop()
     fb, lb = [a.copy() for a in b.download()]
     b.upload('seed')
     ms_plain = timed(lambda: b.plain_launches(stream=stream.cuda_stream), 1)
     fp, lp = b.download()
     identical = bool(np.array_equal(fb, fp, equal_nan=True) and np.array_equal(lb, lp))
+    peak = ctypes_peak(ctx)
+    pt_own = np.repeat(b.turns.astype(np.int64), b.particles)
+    lb64 = lb.astype(np.int64)
+    tracked = float(np.where(lb64 < pt_own, lb64 + 1, pt_own).sum())
+    fl = b.prog.flops_fast if args.mode == 'fma' else b.prog.flops
+    achieved = fl * tracked / (ms_batch / 1e3) / 1e9
     line = {'metric': 'FP64 particle*element*turns/s', 'value': pet / (ms_batch / 1e3),
             'unit': 'particle*element*turns/s', 'n_gpus': 1, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': ms_batch, 'higher_is_better': True,
@@ -409,9 +420,15 @@ def bench_c4(args):
                                    f'particles log-uniform 256-8192, turns U(1000, 4096) // '
                                    f'{args.turn_div}', 'particles': b.n, 'seeds': S,
                        'mode': args.mode, 'tuning': tuning},
+            'roofline': {'bound': 'fp64', 'achieved': achieved, 'peak': peak, 'unit': 'GFLOP/s',
+                         'frac': achieved / peak if peak else None, 'traffic': None,
+                         'flops_per_particle_turn': fl,
+                         'peak_source': 'measured live: ufo_fp64_peak'},
             'plain_one_launch_per_seed': {'value': pet / (ms_plain / 1e3), 'ms': ms_plain},
             'speedup_batched_vs_plain': ms_plain / ms_batch,
             'identical_results': identical, 'gpu_launches': launches}
+    if clk:
+        line['clocks'] = clk
     print(json.dumps(line), flush=True)
 
 
@@ -525,6 +542,80 @@ def _normwise(g, fd):
     return (np.max(np.abs(g - fd), axis=1) / np.max(np.abs(fd), axis=1)).tolist()
 
 
+def _c5_multiturn(args, u, W, torch, ctx, stream, model, ring, params, vals, rng):
+    """d/dk of the summed final amplitudes of 4,096 particles after 1,024 turns
+    (checkpoints every 64) against central FD through the tracking kernel."""
+    P = len(vals)
+    launches = 0
+    Np, T, ck = 4096, 1024, 64
+    coords = W.c2_beam(Np, seed=3)
+    o = 1.0 / (coords[:, 5] + 1.0)
+    eng = model.engine(vals)
+    # particles on chaotic (resonant) orbits have no usable derivative over
+    # 1,024 turns: a 1e-9 m displacement grows exponentially there.  They are
+    # excluded from the objective (a fixed mask, not differentiated).
+    pair = np.concatenate([coords[:, :4], coords[:, :4] + [1e-9, 0, 0, 0]])
+    zp, _ = eng.forward(pair, np.concatenate([o, o]), T)
+    growth = np.max(np.abs(zp[Np:, :4] - zp[:Np, :4]), axis=1) / 1e-9
+    mask = growth < 1e4
+    eng.device_ms, eng.launches = 0.0, 0
+    t0 = time.perf_counter()
+    zT, st = eng.forward(coords[:, :4], o, T, ck=ck)
+    zbar = np.zeros((Np, 4))
+    zbar[:, 0] = 2 * zT[:, 0] * mask
+    zbar[:, 2] = 2 * zT[:, 2] * mask
+    _, gp = eng.reverse(st, zbar)  # per particle [Np, P]
+    g = gp.sum(axis=0)
+    wall_mt = time.perf_counter() - t0
+    dev_mt = eng.device_ms
+    launches += eng.launches
+    del st
+    torch.cuda.empty_cache()
+    m = args.c5_fd_params
+    idx = np.sort(rng.choice(P, m, replace=False))
+    hm = 1e-7 * np.abs(vals[idx])
+    rows_m = np.repeat(vals[None], 2 * m, 0)
+    rows_m[0::2][np.arange(m), idx] += hm
+    rows_m[1::2][np.arange(m), idx] -= hm
+    b = u.TrackBatch(ring, params, rows_m, [Np] * (2 * m), [T] * (2 * m),
+                     flags=u.KICK | u.FMA, context=ctx)
+    b.coords[:] = np.tile(coords, (2 * m, 1))
+    b.upload()
+    b.capture()
+    b.launch(stream=stream.cuda_stream)  # warm-up (graph upload)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = ctx.launches()
+    e0.record(stream)
+    b.launch(stream=stream.cuda_stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches += ctx.launches() - l0
+    dev_fdm = e0.elapsed_time(e1)
+    fin, lost = b.download()
+    ampp = (fin[:, 0] ** 2 + fin[:, 2] ** 2).reshape(2 * m, Np) * mask[None]
+    fdp = (ampp[0::2] - ampp[1::2]) / (2 * hm[:, None])  # per particle [m, Np]
+    fdm = fdp.sum(axis=1)
+    rel = np.abs(g[idx] - fdm) / np.abs(fdp).sum(axis=1)
+    pp = np.abs(gp[:, idx].T - fdp)[:, mask] / np.maximum(np.abs(fdp[:, mask]), 1e-300)
+    fd_full = dev_fdm * P / m
+    out = {
+        'particles': Np, 'turns': T, 'checkpoint_every': ck,
+        'regular_particles': int(mask.sum()),
+        'adjoint_device_ms': dev_mt, 'adjoint_wall_s': wall_mt,
+        'fd_sample_params': m, 'fd_sample_device_ms': dev_fdm,
+        'fd_all_params_device_ms_scaled': fd_full,
+        'device_cost_ratio': fd_full / dev_mt,
+        'fd_lost_particles': int(np.sum(lost < T)),
+        'growth_quantiles_50_99_max': np.quantile(growth, [0.5, 0.99, 1.0]).tolist(),
+        'max_rel_err_vs_central_fd_h1e-7': float(rel.max()),
+        'rel_err_per_param': rel.tolist(),
+        'rel_err_note': '|sum(adjoint - FD)| / sum|per-particle FD| over the regular '
+                        'particles; FD through the tracking kernel (FMA mode)',
+        'per_particle_median_rel_err': float(np.median(pp))}
+    return out, launches
+
+
 def bench_c5(args):
     """Adjoint gradients (C5: the C2 ring with one error seed, 320 k1 + 192 k2)
     against central finite differences, accuracy over all 512 parameters and
@@ -632,74 +723,15 @@ def bench_c5(args):
         'wall_cost_ratio': (wall_f / Sf) / (wall_a / Sa)}
 
     # ---- multi-turn amplitude adjoint
-    Np, T, ck = 4096, 1024, 64
-    coords = W.c2_beam(Np, seed=3)
-    o = 1.0 / (coords[:, 5] + 1.0)
-    eng = model.engine(vals)
-    # particles on chaotic (resonant) orbits have no usable derivative over
-    # 1,024 turns: a 1e-9 m displacement grows exponentially there.  They are
-    # excluded from the objective (a fixed mask, not differentiated).
-    pair = np.concatenate([coords[:, :4], coords[:, :4] + [1e-9, 0, 0, 0]])
-    zp, _ = eng.forward(pair, np.concatenate([o, o]), T)
-    growth = np.max(np.abs(zp[Np:, :4] - zp[:Np, :4]), axis=1) / 1e-9
-    mask = growth < 1e4
-    eng.device_ms, eng.launches = 0.0, 0
-    t0 = time.perf_counter()
-    zT, st = eng.forward(coords[:, :4], o, T, ck=ck)
-    zbar = np.zeros((Np, 4))
-    zbar[:, 0] = 2 * zT[:, 0] * mask
-    zbar[:, 2] = 2 * zT[:, 2] * mask
-    _, gp = eng.reverse(st, zbar)  # per particle [Np, P]
-    g = gp.sum(axis=0)
-    wall_mt = time.perf_counter() - t0
-    dev_mt = eng.device_ms
-    launches += eng.launches
-    del st
-    torch.cuda.empty_cache()
-    m = args.c5_fd_params
-    idx = np.sort(rng.choice(P, m, replace=False))
-    hm = 1e-7 * np.abs(vals[idx])
-    rows_m = np.repeat(vals[None], 2 * m, 0)
-    rows_m[0::2][np.arange(m), idx] += hm
-    rows_m[1::2][np.arange(m), idx] -= hm
-    b = u.TrackBatch(ring, params, rows_m, [Np] * (2 * m), [T] * (2 * m),
-                     flags=u.KICK | u.FMA, context=ctx)
-    b.coords[:] = np.tile(coords, (2 * m, 1))
-    b.upload()
-    b.capture()
-    b.launch(stream=stream.cuda_stream)  # warm-up (graph upload)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    l0 = ctx.launches()
-    e0.record(stream)
-    b.launch(stream=stream.cuda_stream)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    launches += ctx.launches() - l0
-    dev_fdm = e0.elapsed_time(e1)
-    fin, lost = b.download()
-    ampp = (fin[:, 0] ** 2 + fin[:, 2] ** 2).reshape(2 * m, Np) * mask[None]
-    fdp = (ampp[0::2] - ampp[1::2]) / (2 * hm[:, None])  # per particle [m, Np]
-    fdm = fdp.sum(axis=1)
-    rel = np.abs(g[idx] - fdm) / np.abs(fdp).sum(axis=1)
-    pp = np.abs(gp[:, idx].T - fdp)[:, mask] / np.maximum(np.abs(fdp[:, mask]), 1e-300)
-    fd_full = dev_fdm * P / m
-    res['multiturn'] = {
-        'particles': Np, 'turns': T, 'checkpoint_every': ck,
-        'regular_particles': int(mask.sum()),
-        'adjoint_device_ms': dev_mt, 'adjoint_wall_s': wall_mt,
-        'fd_sample_params': m, 'fd_sample_device_ms': dev_fdm,
-        'fd_all_params_device_ms_scaled': fd_full,
-        'device_cost_ratio': fd_full / dev_mt,
-        'fd_lost_particles': int(np.sum(lost < T)),
-        'growth_quantiles_50_99_max': np.quantile(growth, [0.5, 0.99, 1.0]).tolist(),
-        'max_rel_err_vs_central_fd_h1e-7': float(rel.max()),
-        'rel_err_per_param': rel.tolist(),
-        'rel_err_note': '|sum(adjoint - FD)| / sum|per-particle FD| over the regular '
-                        'particles; FD through the tracking kernel (FMA mode)',
-        'per_particle_median_rel_err': float(np.median(pp))}
+    if not args.c5_skip_multiturn:
+        res['multiturn'], n_l = _c5_multiturn(args, u, W, torch, ctx, stream, model, ring,
+                                              params, vals, rng)
+        launches += n_l
     clk = clocks.stop()
-    ratio = min(res['optics_batched']['device_cost_ratio'], res['multiturn']['device_cost_ratio'])
+    ratios = [res['optics_batched']['device_cost_ratio']]
+    if res.get('multiturn'):
+        ratios.append(res['multiturn']['device_cost_ratio'])
+    ratio = min(ratios)
     line = {'metric': 'adjoint gradient cost advantage over central finite differences '
                       '(device time, all 512 parameters)',
             'value': ratio, 'unit': 'x', 'n_gpus': 1, 'steps': 1, 'warmup': 1,

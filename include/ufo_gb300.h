@@ -153,8 +153,11 @@ void ufo_graph_destroy(ufo_graph *graph);
  *     f64[turns/ck+1][20][J] every `ck` turns (NULL: none)
  *   ufo_diff_reverse: the checkpoints of the forward call, output cotangents
  *     zbar f64[J][4] (and Tbar f64[J][16]) -> zbar0 f64[J][4], parameter
- *     cotangents pbar f64[n_params][J]; scratch tape
- *     f64[ck][kicks_per_turn][nf][J], nf = 10 with `tangent`, else 2.
+ *     cotangents pbar f64[n_params][J].  Scratch tape
+ *     f64[tape_segments][ck][kicks_per_turn][nf][J]: with `tangent` nf = 10 and
+ *     one segment is taped at a time (tape_segments = 1 suffices); without it
+ *     nf = 4 and tape_segments checkpoint segments are re-tracked in parallel
+ *     (G x J jobs) before they are reversed, so a larger tape shortens the pass.
  */
 int ufo_diff_forward(const int32_t *ops, int n_ops, const double *tab, int64_t tab_stride,
                      const int32_t *seed, int n_params, int kicks_per_turn, int n_jobs,
@@ -163,8 +166,8 @@ int ufo_diff_forward(const int32_t *ops, int n_ops, const double *tab, int64_t t
 int ufo_diff_reverse(const int32_t *ops, int n_ops, const double *tab, int64_t tab_stride,
                      const int32_t *seed, int n_params, int kicks_per_turn, int n_jobs,
                      const double *o, int turns, int ck, int tangent, const double *ckpt,
-                     const double *zbar, const double *Tbar, double *tape, double *zbar0,
-                     double *pbar, void *stream);
+                     const double *zbar, const double *Tbar, double *tape, int tape_segments,
+                     double *zbar0, double *pbar, void *stream);
 
 /* Kernel launches issued by this library since the context was created.
  * Diagnostic; no reference counterpart. */

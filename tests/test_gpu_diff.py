@@ -229,3 +229,25 @@ def test_tunes_and_gradients_vs_reference_optics_method():
     xi_ref = [(q1[0] - qx) / d, (q1[1] - qy) / d]
     xi = out[6:8].detach().numpy()
     assert np.all(np.abs(xi - xi_ref) <= 1e-2 * np.abs(xi)), (xi, xi_ref)
+
+
+def test_segment_grouping_is_bit_identical():
+    """The plain reverse pass re-tracks G checkpoint segments at once; the
+    group size (set by the tape budget) must not change any result bit."""
+    import ufo_gb300 as u
+    from ufo_gb300 import diff as D, workloads as W
+    ring = _ring()
+    params, vals = _params(ring)
+    coords = W.c2_beam(64, seed=3)
+    o = 1 / (1 + coords[:, 5])
+    out = []
+    for budget in (1, 2 * 16 * 2560 * 4 * 64 * 8, 64 << 30):
+        eng = D.DiffEngine(D.DiffProgram(ring, u.KICK, params, vals), tape_budget=budget)
+        zT, st = eng.forward(coords[:, :4], o, 90, ck=16)
+        zbar = np.zeros((64, 4))
+        zbar[:, 0] = 2 * zT[:, 0]
+        zbar[:, 2] = 2 * zT[:, 2]
+        out.append(eng.reverse(st, zbar) + (eng.last_tape_segments,))
+    assert [r[2] for r in out] == [1, 2, 6]
+    for zb, pb, _ in out[1:]:
+        assert np.array_equal(zb, out[0][0]) and np.array_equal(pb, out[0][1])

@@ -59,7 +59,8 @@ SIGNATURES = {
     'ufo_diff_forward': [P, ctypes.c_int, P, I64, P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                          P, P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P],
     'ufo_diff_reverse': [P, ctypes.c_int, P, I64, P, ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                         P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, P, P, P, P],
+                         P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P, P, P, P, ctypes.c_int,
+                         P, P, P],
     'ufo_track_noalloc': [P, ctypes.c_int, P, I64, ctypes.c_int, ctypes.c_int, P, P, P, I64,
                           ctypes.c_int, ctypes.c_int, ctypes.c_int, I64, ctypes.c_int, P, P, P,
                           P],

@@ -15,11 +15,18 @@
 //
 // diff_forward: z (and optionally the 4x4 tangent T = dz/dz0) through `turns`
 //   turns, writing the state (and T) every `ck` turns as checkpoints.
-// diff_reverse: given the output cotangents zbar (and Tbar), walks the
-//   checkpoint segments backwards: each segment is re-tracked once onto a tape
-//   (x, y and the x/y rows of T at every kick of every turn of the segment) and
-//   then reversed turn by turn; accumulates the cotangent of the start state
-//   and of every element parameter.
+// Reverse pass, given the output cotangents zbar (and Tbar), over the
+//   checkpoint segments from the last to the first:
+//   * plain (multi-turn) mode: diff_tape re-tracks G segments at once
+//     (G x J independent jobs: the segments only need their checkpoints) onto
+//     a "rich" tape holding x, y and S'(z) at every kick; diff_reverse_plain
+//     then walks those G segments backwards, job by job, with the cheap
+//     reverse kick the stored S' allows.  The cotangent state is carried in
+//     zbar0 from one group of segments to the next.
+//   * tangent mode (optics, one turn): diff_reverse re-tracks each segment
+//     onto a tape of x, y and the x/y rows of T and reverses it in one kernel.
+//   Both accumulate the cotangent of the start state and of every element
+//   parameter.
 // Per-job buffers that grow with the work (checkpoints, tape, parameter
 // cotangents) are laid out job-fastest, so a warp's 32 jobs touch 32
 // consecutive doubles.  Arithmetic is FP64 with fused multiply-adds (gradients
@@ -54,7 +61,7 @@ struct DiffArgs {
   double *zT;             // [job][20] final state (+T)
   const double *zbar;     // [job][4] output cotangents
   const double *Tbar;     // [job][16] (tangent only)
-  double *tape;           // [ck][kicks_per_turn][nf][job], nf = 10 (tangent) or 2
+  double *tape;           // [G][ck][kicks_per_turn][nf][job], nf = 10 (tangent) or 4
   double *zbar0;          // [job][4] cotangent of the start state
   double *pbar;           // [n_params][job]
 };
@@ -128,17 +135,31 @@ __device__ __forceinline__ void fwd_kick(St &s, const double *a, int M, double o
   s.py += o * si;
 }
 
-// tape slot of field f of kick k in turn tt of the segment
+// tape slot of field f of kick k in turn tt (counted from the start of the
+// group of segments being taped); rich-tape fields: x, y, Re S', Im S'
 __device__ __forceinline__ int64_t tidx(const DiffArgs &a, int tt, int k, int f, int nf, int j) {
   return ((static_cast<int64_t>(tt) * a.kicks_per_turn + k) * nf + f) * a.n_jobs + j;
 }
 
+// forward kick that also records x, y and S'(z) on the rich tape
+__device__ __forceinline__ void fwd_kick_rich(St &s, const double *a, int M, double o, double *t0,
+                                              int64_t stride) {
+  double sr, si, ar, ai, br, bi;
+  series<1>(a, M, s.x, s.y, sr, si, ar, ai, br, bi);
+  t0[0] = s.x;
+  t0[stride] = s.y;
+  t0[2 * stride] = o * ar;
+  t0[3 * stride] = o * ai;
+  s.px -= o * sr;
+  s.py += o * si;
+}
+
 // one turn forward; with `tape` the state at every kick is recorded as turn
-// `tt` of the segment
+// `tt` of the group (tangent: x, y and the x/y rows of T; plain: x, y, S'/o)
 __device__ void turn_forward(St &s, const DiffArgs &a, const double *T0, double o, bool tangent,
                              int j, int tt, bool tape) {
   int kidx = 0;
-  const int nf = tangent ? 10 : 2;
+  const int nf = tangent ? 10 : 4;
   for (int i = 0; i < a.n_ops; ++i) {
     const DOp op = a.ops[i];
     const double *c = T0 + op.toff;
@@ -171,17 +192,22 @@ __device__ void turn_forward(St &s, const DiffArgs &a, const double *T0, double 
         const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2);
         if (tp) fwd_drift(s, Lo, tangent);
         for (int sl = 0; sl < N; ++sl) {
+          const int k = kidx++;
+          if (tape && !tangent) {
+            fwd_kick_rich(s, c + KHDR, op.M, oo, a.tape + tidx(a, tt, k, 0, nf, j), a.n_jobs);
+            if (tp && W != 0.0) fwd_weak(s, W, tangent);
+            if (tp) fwd_drift(s, sl < N - 1 ? Li : Lo, tangent);
+            continue;
+          }
           if (tape) {
             double *t = a.tape;
-            const int k = kidx++;
             t[tidx(a, tt, k, 0, nf, j)] = s.x;
             t[tidx(a, tt, k, 1, nf, j)] = s.y;
-            if (tangent)
 #pragma unroll
-              for (int q = 0; q < 4; ++q) {
-                t[tidx(a, tt, k, 2 + q, nf, j)] = s.T[q];
-                t[tidx(a, tt, k, 6 + q, nf, j)] = s.T[8 + q];
-              }
+            for (int q = 0; q < 4; ++q) {
+              t[tidx(a, tt, k, 2 + q, nf, j)] = s.T[q];
+              t[tidx(a, tt, k, 6 + q, nf, j)] = s.T[8 + q];
+            }
           }
           fwd_kick(s, c + KHDR, op.M, oo, tangent);
           if (tp && W != 0.0) fwd_weak(s, W, tangent);
@@ -235,13 +261,10 @@ __device__ __forceinline__ void zpow(double x, double y, int n, double &zr, doub
 __device__ __forceinline__ void rev_kick(Bar &b, const DiffArgs &a, int tt, int k, int j,
                                          const double *co, int M, double o, bool tangent, int pm,
                                          double &g0, double &g1) {
-  const int nf = tangent ? 10 : 2;
+  const int nf = 10;
   const double x = a.tape[tidx(a, tt, k, 0, nf, j)], y = a.tape[tidx(a, tt, k, 1, nf, j)];
   double s0r, s0i, a1, b1, a2, b2;
-  if (tangent)
-    series<2>(co, M, x, y, s0r, s0i, a1, b1, a2, b2);
-  else
-    series<1>(co, M, x, y, s0r, s0i, a1, b1, a2, b2);
+  series<2>(co, M, x, y, s0r, s0i, a1, b1, a2, b2);
   a1 *= o;
   b1 *= o;
   // state: px' = px - Re S, py' = py + Im S
@@ -332,6 +355,99 @@ __device__ void turn_reverse(Bar &b, const DiffArgs &a, const double *T0, double
   }
 }
 
+// z^pm for the parameter weight of the reverse kick: closed forms for the
+// quadrupole and sextupole orders
+__device__ __forceinline__ void zpow_small(double x, double y, int pm, double &zr, double &zi) {
+  if (pm == 1) {
+    zr = x;
+    zi = y;
+  } else if (pm == 2) {
+    zr = fma(x, x, -y * y);
+    zi = 2.0 * x * y;
+  } else if (pm == 0) {
+    zr = 1.0;
+    zi = 0.0;
+  } else {
+    zpow(x, y, pm, zr, zi);
+  }
+}
+
+// reverse of one plain kick from the rich tape (x, y, S'): no polynomial
+// evaluation; adds the parameter cotangent of weight z^pm / o to g0
+__device__ __forceinline__ void rev_kick_rich(Bar &b, const double *t0, int64_t stride, int pm,
+                                              double &g0) {
+  const double a1 = t0[2 * stride], b1 = t0[3 * stride];
+  const double pxb = b.px, pyb = b.py;
+  b.x = fma(-pxb, a1, fma(pyb, b1, b.x));
+  b.y = fma(pxb, b1, fma(pyb, a1, b.y));
+  if (pm >= 0) {
+    double zr, zi;
+    zpow_small(t0[0], t0[stride], pm, zr, zi);
+    g0 = fma(-pxb, zr, fma(pyb, zi, g0));
+  }
+}
+
+// the reverse walk reads the tape backwards from HBM with one warp per SM:
+// the x, y, S' of the kick PF kicks ahead are requested into L1 first
+constexpr int PF = 16;
+
+__device__ __forceinline__ void prefetch_l1(const double *p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
+
+// reverse of turn `tt` of the group from the rich tape (plain mode)
+__device__ void turn_reverse_plain(Bar &b, const DiffArgs &a, const double *T0, double o, int j,
+                                   int tt) {
+  int kidx = a.kicks_per_turn;
+  const int64_t qbase = static_cast<int64_t>(tt) * a.kicks_per_turn;
+  for (int i = a.n_ops - 1; i >= 0; --i) {
+    const DOp op = a.ops[i];
+    const double *c = T0 + op.toff;
+    const double oo = op.achro ? 1.0 : o;
+    switch (op.kind) {
+      case D_DRIFT:
+        rev_drift(b, __ldg(c), false);
+        break;
+      case D_ALIGN:
+        break;
+      case D_EDGE: {
+        const double curv = __ldg(c) * oo;
+        b.x = fma(b.px * curv, __ldg(c + 1), b.x);
+        b.y = fma(-(b.py * curv), __ldg(c + 2), b.y);
+        break;
+      }
+      case D_KICK:
+      case D_TEAPOT: {
+        const bool tp = op.kind == D_TEAPOT;
+        const int N = tp ? op.N : 1;
+        const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2);
+        const int pm = op.pslot >= 0 ? op.pm : -1;
+        double g0 = 0.0;
+        for (int sl = N - 1; sl >= 0; --sl) {
+          if (tp) rev_drift(b, sl < N - 1 ? Li : Lo, false);
+          if (tp && W != 0.0) rev_weak(b, W, false);
+          --kidx;
+          const int64_t q = qbase + kidx - PF;  // position in the group's kick sequence
+          if (q >= 0) {
+            const double *pf = a.tape + q * 4 * a.n_jobs + j;
+#pragma unroll
+            for (int f = 0; f < 4; ++f) prefetch_l1(pf + f * static_cast<int64_t>(a.n_jobs));
+          }
+          rev_kick_rich(b, a.tape + tidx(a, tt, kidx, 0, 4, j), a.n_jobs, pm, g0);
+        }
+        if (tp) rev_drift(b, Lo, false);
+        if (op.pslot >= 0) {  // dS/dc = o z^pm / pm!
+          double &p = a.pbar[static_cast<int64_t>(op.pslot) * a.n_jobs + j];
+          p = fma(g0 * oo, __ldg(c + 3), p);
+        }
+        break;
+      }
+      default:
+        break;
+    }
+  }
+}
+
 __device__ void save_ckpt(const St &s, const DiffArgs &a, int c, int j, bool tangent) {
   double *d = a.ckpt + static_cast<int64_t>(c) * 20 * a.n_jobs + j;
   d[0] = s.x;
@@ -400,6 +516,44 @@ __global__ void diff_reverse(DiffArgs a) {
   a.zbar0[4 * j + 3] = b.py;
 }
 
+// plain mode, step 1: G segments [sg0, sg0 + G) re-tracked from their
+// checkpoints onto the rich tape, one thread per (segment, job), jobs fastest
+__global__ void diff_tape(DiffArgs a, int sg0, int G) {
+  const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (t >= static_cast<int64_t>(G) * a.n_jobs) return;
+  const int g = static_cast<int>(t / a.n_jobs), j = static_cast<int>(t % a.n_jobs);
+  const int sg = sg0 + g;
+  const int t0 = sg * a.ck;
+  if (t0 >= a.turns) return;
+  const int t1 = min(a.turns, t0 + a.ck);
+  const double o = a.o[j];
+  const double *T0 = a.tab + (a.seed ? static_cast<int64_t>(a.seed[j]) : 0) * a.tab_stride;
+  St s;
+  load_ckpt(s, a, sg, j, false);
+  for (int tt = t0; tt < t1; ++tt) turn_forward(s, a, T0, o, false, j, g * a.ck + (tt - t0), true);
+}
+
+// plain mode, step 2: the segments [sg0, sg_hi] reversed from the tape, one
+// thread per job; the cotangent of the state is read from and written back to
+// zbar0
+__global__ void diff_reverse_plain(DiffArgs a, int sg0, int sg_hi) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= a.n_jobs) return;
+  const double o = a.o[j];
+  const double *T0 = a.tab + (a.seed ? static_cast<int64_t>(a.seed[j]) : 0) * a.tab_stride;
+  Bar b;
+  b.x = a.zbar0[4 * j]; b.px = a.zbar0[4 * j + 1]; b.y = a.zbar0[4 * j + 2];
+  b.py = a.zbar0[4 * j + 3];
+  for (int sg = sg_hi; sg >= sg0; --sg) {
+    const int t0 = sg * a.ck;
+    const int t1 = min(a.turns, t0 + a.ck);
+    for (int tt = t1 - 1; tt >= t0; --tt)
+      turn_reverse_plain(b, a, T0, o, j, (sg - sg0) * a.ck + (tt - t0));
+  }
+  a.zbar0[4 * j] = b.x; a.zbar0[4 * j + 1] = b.px; a.zbar0[4 * j + 2] = b.y;
+  a.zbar0[4 * j + 3] = b.py;
+}
+
 }  // namespace ufo_diff
 
 // ---------------------------------------------------------------- C ABI
@@ -408,12 +562,27 @@ extern "C" {
 // All pointers are device pointers; `ops` int32[n_ops][8] (DOp), `tab` f64.
 // Asynchronous on `stream`.  Returns 0, -1 (bad arguments) or -2 (launch
 // error).
+// the kernels use no shared memory: give the whole on-chip store to L1, where
+// the opcode list and one seed's constants (~200 kB for a 1,000-element ring)
+// then stay resident
+static void prefer_l1() {
+  static bool done = false;
+  if (done) return;
+  cudaFuncSetAttribute(ufo_diff::diff_forward, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+  cudaFuncSetAttribute(ufo_diff::diff_reverse, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+  cudaFuncSetAttribute(ufo_diff::diff_tape, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+  cudaFuncSetAttribute(ufo_diff::diff_reverse_plain,
+                       cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+  done = true;
+}
+
 int ufo_diff_forward(const int32_t *ops, int n_ops, const double *tab, int64_t tab_stride,
                      const int32_t *seed, int n_params, int kicks_per_turn, int n_jobs,
                      const double *z0, const double *o, int turns, int ck, int tangent,
                      double *ckpt, double *zT, void *stream) {
   if (n_jobs <= 0) return 0;
   if (!ops || n_ops < 0 || !tab || !z0 || !o || !zT || turns < 0 || ck < 1) return -1;
+  prefer_l1();
   ufo_diff::DiffArgs a{};
   a.ops = reinterpret_cast<const ufo_diff::DOp *>(ops);
   a.n_ops = n_ops;
@@ -438,12 +607,13 @@ int ufo_diff_forward(const int32_t *ops, int n_ops, const double *tab, int64_t t
 int ufo_diff_reverse(const int32_t *ops, int n_ops, const double *tab, int64_t tab_stride,
                      const int32_t *seed, int n_params, int kicks_per_turn, int n_jobs,
                      const double *o, int turns, int ck, int tangent, const double *ckpt,
-                     const double *zbar, const double *Tbar, double *tape, double *zbar0,
-                     double *pbar, void *stream) {
+                     const double *zbar, const double *Tbar, double *tape, int tape_segments,
+                     double *zbar0, double *pbar, void *stream) {
   if (n_jobs <= 0) return 0;
   if (!ops || n_ops < 0 || !tab || !o || !ckpt || !zbar || !tape || !zbar0 ||
-      (n_params > 0 && !pbar) || turns < 1 || ck < 1 || (tangent && !Tbar))
+      (n_params > 0 && !pbar) || turns < 1 || ck < 1 || (tangent && !Tbar) || tape_segments < 1)
     return -1;
+  prefer_l1();
   ufo_diff::DiffArgs a{};
   a.ops = reinterpret_cast<const ufo_diff::DOp *>(ops);
   a.n_ops = n_ops;
@@ -464,8 +634,29 @@ int ufo_diff_reverse(const int32_t *ops, int n_ops, const double *tab, int64_t t
   a.zbar0 = zbar0;
   a.pbar = pbar;
   const int tpb = 32;
-  ufo_diff::diff_reverse<<<(n_jobs + tpb - 1) / tpb, tpb, 0, static_cast<cudaStream_t>(stream)>>>(a);
-  return cudaGetLastError() == cudaSuccess ? 0 : -2;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (tangent) {
+    ufo_diff::diff_reverse<<<(n_jobs + tpb - 1) / tpb, tpb, 0, st>>>(a);
+    return cudaGetLastError() == cudaSuccess ? 0 : -2;
+  }
+  // plain mode: groups of up to tape_segments segments, last group first
+  if (n_params > 0 &&
+      cudaMemsetAsync(pbar, 0, sizeof(double) * n_params * static_cast<size_t>(n_jobs), st) !=
+          cudaSuccess)
+    return -2;
+  if (cudaMemcpyAsync(zbar0, zbar, sizeof(double) * 4 * static_cast<size_t>(n_jobs),
+                      cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+    return -2;
+  const int last_seg = (turns - 1) / ck;
+  for (int hi = last_seg; hi >= 0; hi -= tape_segments) {
+    const int lo = hi - tape_segments + 1 < 0 ? 0 : hi - tape_segments + 1;
+    const int G = hi - lo + 1;
+    const int64_t threads = static_cast<int64_t>(G) * n_jobs;
+    ufo_diff::diff_tape<<<static_cast<unsigned>((threads + tpb - 1) / tpb), tpb, 0, st>>>(a, lo, G);
+    ufo_diff::diff_reverse_plain<<<(n_jobs + tpb - 1) / tpb, tpb, 0, st>>>(a, lo, hi);
+    if (cudaGetLastError() != cudaSuccess) return -2;
+  }
+  return 0;
 }
 
 }  // extern "C"

@@ -189,9 +189,13 @@ class DiffEngine:
     torch's current stream; ``device_ms`` and ``launches`` accumulate their
     CUDA-event time and count."""
 
-    def __init__(self, dprog, device=0):
+    def __init__(self, dprog, device=0, tape_budget=None):
         torch = _torch()
         from . import capi
+        # bytes of device memory for the reverse tape; default: 40% of the free
+        # memory at reverse time, at most 128 GiB (more memory = more
+        # checkpoint segments re-tracked in parallel)
+        self.tape_budget = tape_budget
         self.capi = capi
         self.lib = capi.load()
         self.dev = torch.device('cuda', device)
@@ -254,16 +258,25 @@ class DiffEngine:
         if tangent:
             Tb = torch.as_tensor(np.ascontiguousarray(Tbar, np.float64).reshape(J, 16),
                                  device=self.dev)
-        nf = 10 if tangent else 2
-        tape = torch.empty((min(ck, turns), max(1, self.p.kicks_per_turn), nf, J),
+        nf = 10 if tangent else 4
+        seg_len = min(ck, turns)
+        seg_bytes = seg_len * max(1, self.p.kicks_per_turn) * nf * J * 8
+        n_seg = (turns - 1) // ck + 1
+        budget = self.tape_budget
+        if budget is None:
+            free, _ = torch.cuda.mem_get_info(self.dev)
+            budget = min(128 << 30, int(0.4 * free))
+        G = 1 if tangent else int(max(1, min(n_seg, budget // max(1, seg_bytes))))
+        tape = torch.empty((G, seg_len, max(1, self.p.kicks_per_turn), nf, J),
                            dtype=torch.float64, device=self.dev)
+        self.last_tape_segments = G
         zbar0 = torch.empty((J, 4), dtype=torch.float64, device=self.dev)
         pbar = torch.empty((max(1, self.p.n_params), J), dtype=torch.float64, device=self.dev)
         self._run(lambda st: self.lib.ufo_diff_reverse(
             self._ptr(self.ops), self.ops.shape[0], self._ptr(self.tab), self.p.tab_stride,
             self._ptr(sd), self.p.n_params, self.p.kicks_per_turn, J, self._ptr(o), int(turns),
             int(ck), int(bool(tangent)), self._ptr(ckpt), self._ptr(zbar), self._ptr(Tb),
-            self._ptr(tape), self._ptr(zbar0), self._ptr(pbar), st), 'ufo_diff_reverse')
+            self._ptr(tape), G, self._ptr(zbar0), self._ptr(pbar), st), 'ufo_diff_reverse')
         pb = pbar[:self.p.n_params]
         pb = pb.sum(dim=1) if sum_jobs else pb.T
         return zbar0.cpu().numpy(), pb.cpu().numpy()
