@@ -21,6 +21,12 @@ Printed (rank 0, one JSON line):
              oracle port when that is absent, on a bounded sample on the host
              cores
 --impl reference times the reference's CPU implementation the same way.
+
+Other workloads (--workload): c3 dynamic-aperture scan (persistent vs plain
+kernel, sorted and shuffled grids), c4 batched error seeds (one autotuned
+CUDA-graph launch vs one launch per seed), c5 adjoint gradients against central
+finite differences (accuracy and device/wall cost).  The c2 line also carries
+the strict-mode (bit-identical) and Yoshida-4 measurements of the same ring.
 """
 import argparse
 import json
