@@ -154,7 +154,8 @@ void ufo_graph_destroy(ufo_graph *graph);
  *   ufo_diff_reverse: the checkpoints of the forward call, output cotangents
  *     zbar f64[J][4] (and Tbar f64[J][16]) -> zbar0 f64[J][4], parameter
  *     cotangents pbar f64[n_params][J].  Scratch tape
- *     f64[tape_segments][ck][kicks_per_turn][nf][J]: with `tangent` nf = 10 and
+ *     f64[tape_segments * ck][ceil(J/32)][kicks_per_turn][nf][32] (warp-blocked,
+ *     16-byte aligned): with `tangent` nf = 10 and
  *     one segment is taped at a time (tape_segments = 1 suffices); without it
  *     nf = 4 and tape_segments checkpoint segments are re-tracked in parallel
  *     (G x J jobs) before they are reversed, so a larger tape shortens the pass.

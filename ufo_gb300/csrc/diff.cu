@@ -61,7 +61,7 @@ struct DiffArgs {
   double *zT;             // [job][20] final state (+T)
   const double *zbar;     // [job][4] output cotangents
   const double *Tbar;     // [job][16] (tangent only)
-  double *tape;           // [G][ck][kicks_per_turn][nf][job], nf = 10 (tangent) or 4
+  double *tape;           // [G*ck][warp][kicks_per_turn][nf][lane], nf = 10 (tangent) or 4
   double *zbar0;          // [job][4] cotangent of the start state
   double *pbar;           // [n_params][job]
 };
@@ -136,9 +136,14 @@ __device__ __forceinline__ void fwd_kick(St &s, const double *a, int M, double o
 }
 
 // tape slot of field f of kick k in turn tt (counted from the start of the
-// group of segments being taped); rich-tape fields: x, y, Re S', Im S'
+// group of segments being taped); rich-tape fields: x, y, Re S', Im S'.
+// Warp-blocked: one warp's values for one turn are a contiguous run (the
+// reverse walk prefetches them in bulk), a kick's field a 256-byte line.
+constexpr int TLANES = 32;
 __device__ __forceinline__ int64_t tidx(const DiffArgs &a, int tt, int k, int f, int nf, int j) {
-  return ((static_cast<int64_t>(tt) * a.kicks_per_turn + k) * nf + f) * a.n_jobs + j;
+  const int64_t warps = (a.n_jobs + TLANES - 1) / TLANES;
+  return (((static_cast<int64_t>(tt) * warps + j / TLANES) * a.kicks_per_turn + k) * nf + f) *
+             TLANES + (j % TLANES);
 }
 
 // forward kick that also records x, y and S'(z) on the rich tape
@@ -194,7 +199,7 @@ __device__ void turn_forward(St &s, const DiffArgs &a, const double *T0, double 
         for (int sl = 0; sl < N; ++sl) {
           const int k = kidx++;
           if (tape && !tangent) {
-            fwd_kick_rich(s, c + KHDR, op.M, oo, a.tape + tidx(a, tt, k, 0, nf, j), a.n_jobs);
+            fwd_kick_rich(s, c + KHDR, op.M, oo, a.tape + tidx(a, tt, k, 0, nf, j), TLANES);
             if (tp && W != 0.0) fwd_weak(s, W, tangent);
             if (tp) fwd_drift(s, sl < N - 1 ? Li : Lo, tangent);
             continue;
@@ -387,19 +392,33 @@ __device__ __forceinline__ void rev_kick_rich(Bar &b, const double *t0, int64_t 
   }
 }
 
-// the reverse walk reads the tape backwards from HBM with one warp per SM:
-// the x, y, S' of the kick PF kicks ahead are requested into L1 first
-constexpr int PF = 16;
+// The reverse walk reads the tape backwards from HBM with one warp per SM,
+// one dependent access per kick.  Lane 0 asks the copy engine to bring the
+// warp's next chunks (CHUNK kicks, 64 KiB) into L2 ahead of use: fire and
+// forget, nothing waits on it.
+constexpr int CHUNK = 64;
 
-__device__ __forceinline__ void prefetch_l1(const double *p) {
-  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+__device__ __forceinline__ void prefetch_l2_bulk(const double *p, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+// chunk [k0, k0 + CHUNK) of turn tt (clipped at 0) of this lane's warp
+__device__ __forceinline__ void prefetch_chunk(const DiffArgs &a, int tt, int k0, int j) {
+  const int lo = k0 < 0 ? 0 : k0;
+  const int hi = min(k0 + CHUNK, a.kicks_per_turn);  // stay inside this warp's turn
+  if (hi <= lo || (j % TLANES) != 0) return;
+  prefetch_l2_bulk(a.tape + tidx(a, tt, lo, 0, 4, j),
+                   static_cast<uint32_t>((hi - lo) * 4 * TLANES * sizeof(double)));
 }
 
 // reverse of turn `tt` of the group from the rich tape (plain mode)
 __device__ void turn_reverse_plain(Bar &b, const DiffArgs &a, const double *T0, double o, int j,
                                    int tt) {
   int kidx = a.kicks_per_turn;
-  const int64_t qbase = static_cast<int64_t>(tt) * a.kicks_per_turn;
+  // the first two chunks of this turn's walk (its last kicks)
+  const int top = ((a.kicks_per_turn - 1) / CHUNK) * CHUNK;
+  prefetch_chunk(a, tt, top, j);
+  prefetch_chunk(a, tt, top - CHUNK, j);
   for (int i = a.n_ops - 1; i >= 0; --i) {
     const DOp op = a.ops[i];
     const double *c = T0 + op.toff;
@@ -427,13 +446,9 @@ __device__ void turn_reverse_plain(Bar &b, const DiffArgs &a, const double *T0, 
           if (tp) rev_drift(b, sl < N - 1 ? Li : Lo, false);
           if (tp && W != 0.0) rev_weak(b, W, false);
           --kidx;
-          const int64_t q = qbase + kidx - PF;  // position in the group's kick sequence
-          if (q >= 0) {
-            const double *pf = a.tape + q * 4 * a.n_jobs + j;
-#pragma unroll
-            for (int f = 0; f < 4; ++f) prefetch_l1(pf + f * static_cast<int64_t>(a.n_jobs));
-          }
-          rev_kick_rich(b, a.tape + tidx(a, tt, kidx, 0, 4, j), a.n_jobs, pm, g0);
+          if (kidx % CHUNK == 0 && kidx >= 2 * CHUNK)  // entering a chunk: two ahead
+            prefetch_chunk(a, tt, kidx - 2 * CHUNK, j);
+          rev_kick_rich(b, a.tape + tidx(a, tt, kidx, 0, 4, j), TLANES, pm, g0);
         }
         if (tp) rev_drift(b, Lo, false);
         if (op.pslot >= 0) {  // dS/dc = o z^pm / pm!

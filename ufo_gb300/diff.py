@@ -260,14 +260,15 @@ class DiffEngine:
                                  device=self.dev)
         nf = 10 if tangent else 4
         seg_len = min(ck, turns)
-        seg_bytes = seg_len * max(1, self.p.kicks_per_turn) * nf * J * 8
+        W = (J + 31) // 32  # the tape is warp-blocked: [turn][warp][kick][field][lane]
+        seg_bytes = seg_len * max(1, self.p.kicks_per_turn) * nf * W * 32 * 8
         n_seg = (turns - 1) // ck + 1
         budget = self.tape_budget
         if budget is None:
             free, _ = torch.cuda.mem_get_info(self.dev)
             budget = min(128 << 30, int(0.4 * free))
         G = 1 if tangent else int(max(1, min(n_seg, budget // max(1, seg_bytes))))
-        tape = torch.empty((G, seg_len, max(1, self.p.kicks_per_turn), nf, J),
+        tape = torch.empty((G * seg_len, W, max(1, self.p.kicks_per_turn), nf, 32),
                            dtype=torch.float64, device=self.dev)
         self.last_tape_segments = G
         zbar0 = torch.empty((J, 4), dtype=torch.float64, device=self.dev)
