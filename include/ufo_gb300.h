@@ -123,8 +123,20 @@ int ufo_track_noalloc(const int32_t *ops, int n_ops, const double *d_table, int6
                       int64_t slots, int every, double *d_tracks, uint32_t *d_lost,
                       double *d_final, void *stream);
 
+/* Closed orbits by the reference's Nelder-Mead search (ufo/co.py:18-124, the
+ * ClosedOrbit kernel :146-250): `iterations` steps on the squared one-turn
+ * residual of (x, px, y, py) at z = 0, dp = 0, oodppo = 1, from the simplex
+ * {v, v + 1e-4 e_j}, in the reference's operation order with the strict
+ * one-turn map, so the orbits equal the reference's.  Host buffers:
+ *   start  f64[n][4] first vertex of each orbit (the reference's x/px/y/py
+ *          parameters, zero where absent)
+ *   seed   i32[n] constant-table row of each orbit, or NULL (row 0)
+ *   orbits f64[n][4] out: the best vertex after `iterations` steps */
+int ufo_closed_orbit(ufo_ctx *ctx, const ufo_prog *prog, const double *start,
+                     const int32_t *seed, int64_t n, int iterations, double *orbits);
+
 /* Resident warps per SM of the persistent grid (default 16); set by the
- * autotuner (ufo_gb300/autotune.py).  No reference counterpart. */
+ * autotuner (ufo_gb300/batch.py: autotune).  No reference counterpart. */
 int ufo_ctx_set_tuning(ufo_ctx *ctx, int warps_per_sm);
 
 /* One tracking launch (work-counter reset + persistent kernel over all

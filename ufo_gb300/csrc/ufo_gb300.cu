@@ -241,6 +241,120 @@ __global__ void __launch_bounds__(128) track_plain_kernel(TrackArgs a) {
   store_final(s, a, p);
 }
 
+// ---------------------------------------------------------------- closed orbit
+// The reference's ClosedOrbit (ufo/co.py:18-124, :146-250): per orbit, a fixed
+// number of Nelder-Mead steps (reflection 1, contraction 0.5, expansion 2) on
+// the squared one-turn residual of (x, px, y, py) with z = 0, dp = 0,
+// oodppo = 1, starting from the simplex {v, v + 1e-4 e_j}.  Every step is the
+// reference's, in its IEEE operation order (no contraction), and the one-turn
+// map is the strict interpreter, so the orbits are the reference's bit for
+// bit.  One thread per orbit; the simplex lives in local memory (indexed by
+// the run-time vertex numbers).
+template <bool FULL>
+UFO_DEV double co_residual(const double *v, const TrackArgs &a, const double *tab) {
+  State s{};
+  s.x = v[0]; s.px = v[1]; s.y = v[2]; s.py = v[3];
+  s.z = 0.0; s.dp = 0.0; s.o = 1.0; s.opdp = 1.0;
+  s.turn = 0;
+  s.bad_o = false;
+  one_turn<false, FULL>(s, a, tab, 0);
+  double r = mul(sub(v[0], s.x), sub(v[0], s.x));
+  r = add(r, mul(sub(v[1], s.px), sub(v[1], s.px)));
+  r = add(r, mul(sub(v[2], s.y), sub(v[2], s.y)));
+  r = add(r, mul(sub(v[3], s.py), sub(v[3], s.py)));
+  return r;
+}
+
+UFO_DEV void co_simplex_sum(const double (*sx)[4], double *psum) {
+  for (int j = 0; j < 4; ++j) {
+    psum[j] = 0.0;
+    for (int i = 0; i < 5; ++i) psum[j] = add(psum[j], sx[i][j]);
+  }
+}
+
+// trial vertex through the face opposite `ihi`, scaled by `fac`; replaces
+// `ihi` if better
+template <bool FULL>
+UFO_DEV double co_try(double (*sx)[4], double *y, double *psum, int ihi, double fac,
+                      const TrackArgs &a, const double *tab) {
+  const double fac1 = dvd(sub(1.0, fac), 4.0);
+  const double fac2 = sub(fac1, fac);
+  double t[4];
+  for (int j = 0; j < 4; ++j) t[j] = sub(mul(psum[j], fac1), mul(sx[ihi][j], fac2));
+  const double yt = co_residual<FULL>(t, a, tab);
+  if (yt < y[ihi]) {
+    y[ihi] = yt;
+    for (int j = 0; j < 4; ++j) {
+      psum[j] = add(psum[j], sub(t[j], sx[ihi][j]));
+      sx[ihi][j] = t[j];
+    }
+  }
+  return yt;
+}
+
+template <bool FULL>
+__global__ void __launch_bounds__(32) co_amoeba_kernel(TrackArgs a, const double *start,
+                                                       double *orbits, int iterations) {
+  const int64_t p = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if (p >= a.n) return;
+  const int64_t sd = a.seed ? static_cast<int64_t>(a.seed[p]) : 0;
+  double *out = orbits + 4 * p;
+  if (sd < 0 || sd >= a.n_seeds) {  // seed outside the table: no orbit
+    for (int j = 0; j < 4; ++j) out[j] = __longlong_as_double(0x7ff8000000000000ll);
+    return;
+  }
+  const double *tab = a.table + sd * a.stride;
+  double sx[5][4], y[5], psum[4];
+  for (int i = 0; i < 5; ++i)
+    for (int j = 0; j < 4; ++j) sx[i][j] = start[4 * p + j];
+  for (int j = 0; j < 4; ++j) sx[j + 1][j] = add(sx[j + 1][j], 1e-4);
+  for (int i = 0; i < 5; ++i) y[i] = co_residual<FULL>(sx[i], a, tab);
+  co_simplex_sum(sx, psum);
+  int iter = 0, ilo = 0;
+  while (true) {
+    ilo = 1;
+    int ihi, inhi;
+    if (y[1] > y[2]) {
+      inhi = 2;
+      ihi = 1;
+    } else {
+      inhi = 1;
+      ihi = 2;
+    }
+    for (int i = 0; i < 5; ++i) {
+      if (y[i] < y[ilo]) ilo = i;
+      if (y[i] > y[ihi]) {
+        inhi = ihi;
+        ihi = i;
+      } else if (y[i] > y[inhi] && i != ihi) {
+        inhi = i;
+      }
+    }
+    if (iter >= iterations) break;
+    double yt = co_try<FULL>(sx, y, psum, ihi, -1.0, a, tab);
+    ++iter;
+    if (yt <= y[ilo]) {
+      yt = co_try<FULL>(sx, y, psum, ihi, 2.0, a, tab);
+    } else if (yt >= y[inhi]) {
+      const double ysave = y[ihi];
+      yt = co_try<FULL>(sx, y, psum, ihi, 0.5, a, tab);
+      if (yt >= ysave) {  // shrink towards the best vertex
+        for (int i = 0; i < 5; ++i) {
+          if (i == ilo) continue;
+          for (int j = 0; j < 4; ++j) {
+            psum[j] = mul(add(sx[i][j], sx[ilo][j]), 0.5);
+            sx[i][j] = psum[j];
+          }
+          y[i] = co_residual<FULL>(psum, a, tab);
+        }
+        iter += 4;
+        co_simplex_sum(sx, psum);
+      }
+    }
+  }
+  for (int j = 0; j < 4; ++j) out[j] = sx[ilo][j];
+}
+
 // FP64 pipe peak probe: 8 independent DFMA chains per thread
 __global__ void __launch_bounds__(256) dfma_peak_kernel(double *out, int iters, double b, double c) {
   double a[8];
@@ -841,6 +955,56 @@ struct ufo_graph {
   cudaGraph_t graph;
   cudaGraphExec_t exec;
 };
+
+extern "C" int ufo_closed_orbit(ufo_ctx *ctx, const ufo_prog *prog, const double *start,
+                                const int32_t *seed, int64_t n, int iterations, double *orbits) {
+  int rc = check_track_args(ctx, prog, n, 1, UFO_MODE_TRACK, 0, 1);
+  if (rc) return rc;
+  if (n == 0) return UFO_OK;
+  if (!start || !orbits) return fail(UFO_E_ARG, "null start or orbit buffer");
+  if (iterations < 0) return fail(UFO_E_ARG, "negative iteration count");
+  if (seed) {
+    for (int64_t i = 0; i < n; ++i)
+      if (seed[i] < 0 || seed[i] >= prog->n_seeds)
+        return fail(UFO_E_ARG, "orbit %lld: seed %d outside [0, %d)",
+                    static_cast<long long>(i), seed[i], prog->n_seeds);
+  }
+  UFO_CUDA(cudaSetDevice(ctx->device));
+  cudaStream_t st = ctx->stream;
+  const size_t vb = sizeof(double) * 4 * n;
+  double *d_start = nullptr, *d_orbits = nullptr;
+  int32_t *d_seed = nullptr;
+  auto cleanup = [&]() { cudaFree(d_start); cudaFree(d_orbits); cudaFree(d_seed); };
+  if (cudaMalloc(&d_start, vb) != cudaSuccess || cudaMalloc(&d_orbits, vb) != cudaSuccess ||
+      (seed && cudaMalloc(&d_seed, sizeof(int32_t) * n) != cudaSuccess)) {
+    cleanup();
+    return fail(UFO_E_NOMEM, "device buffers for %lld orbits", static_cast<long long>(n));
+  }
+  cudaError_t e = cudaMemcpyAsync(d_start, start, vb, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && seed)
+    e = cudaMemcpyAsync(d_seed, seed, sizeof(int32_t) * n, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) {
+    cleanup();
+    return cuda_fail(e, "upload");
+  }
+  ufo::TrackArgs a = make_args(prog->ops, prog->n_ops, prog->table, prog->stride, prog->n_seeds,
+                               prog->n_dumps, nullptr, d_seed, nullptr, n, 1, UFO_MODE_TRACK, 0, 0,
+                               1, nullptr, nullptr, nullptr, ctx->queue);
+  const unsigned blocks = static_cast<unsigned>((n + 31) / 32);
+  if (prog->full)
+    ufo::co_amoeba_kernel<true><<<blocks, 32, 0, st>>>(a, d_start, d_orbits, iterations);
+  else
+    ufo::co_amoeba_kernel<false><<<blocks, 32, 0, st>>>(a, d_start, d_orbits, iterations);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    ctx->launches.fetch_add(1);
+    e = cudaMemcpyAsync(orbits, d_orbits, vb, cudaMemcpyDeviceToHost, st);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  cleanup();
+  if (e != cudaSuccess) return cuda_fail(e, "closed orbit");
+  return UFO_OK;
+}
 
 extern "C" int ufo_ctx_set_tuning(ufo_ctx *ctx, int warps_per_sm) {
   if (!ctx) return fail(UFO_E_ARG, "null context");

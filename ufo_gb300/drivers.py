@@ -232,13 +232,20 @@ class StableAperture:
 
 class ClosedOrbit:
     """Closed orbits (x, px, y, py) of the 4D one-turn map at dp = 0
-    (ufo/co.py:146-250).  The reference minimises the squared residual with a
-    fixed number of Nelder-Mead steps; this build solves F(z) = z by Newton
-    iteration, the Jacobian from the tangent map, until the step stops
-    shrinking (at most ``iterations`` steps)."""
+    (ufo/co.py:146-250).
+
+    method='amoeba' (default): the reference's own search, ``iterations``
+    Nelder-Mead steps on the squared one-turn residual, run on the GPU in the
+    reference's operation order: the orbits are the reference's, bit for bit
+    (ufo_closed_orbit).  method='newton': F(z) = z solved by Newton iteration
+    with the Jacobian of the tangent map, until the step stops shrinking (at
+    most ``iterations`` steps): the exact fixed point, to rounding."""
 
     def __init__(self, line, flags=0x00, particles=1000, parameters=None, dp=0., iterations=200,
-                 context=None, options=None):
+                 context=None, options=None, method='amoeba'):
+        if method not in ('amoeba', 'newton'):
+            raise ValueError(f'unknown closed-orbit method {method!r}')
+        self.method = method
         parameters = list(parameters) if parameters is not None else []
         self.ctx = context if context is not None else globals()['context'](0)
         self.flags = flags
@@ -262,9 +269,18 @@ class ClosedOrbit:
         for j, c in enumerate(COORDS[:4]):
             if c in self._names:
                 guess[:, j] = pool[:, self._names.index(c)]
-        orbits, self.residual = tangent.closed_orbit(self.ctx, dprog, guess, seed=seed,
-                                                     fma=bool(self.flags & FMA),
-                                                     max_iter=self.iterations)
+        if self.method == 'amoeba':
+            orbits = np.empty_like(guess)
+            sd = np.ascontiguousarray(seed, dtype=np.int32) if seed is not None else None
+            capi.check(capi.load().ufo_closed_orbit(
+                self.ctx.handle, dprog.handle, capi.ptr(np.ascontiguousarray(guess)),
+                capi.ptr(sd) if sd is not None else None, guess.shape[0], int(self.iterations),
+                capi.ptr(orbits)))
+            self.residual = None
+        else:
+            orbits, self.residual = tangent.closed_orbit(self.ctx, dprog, guess, seed=seed,
+                                                         fma=bool(self.flags & FMA),
+                                                         max_iter=self.iterations)
         self.orbits = orbits.astype(self.orbits.dtype, copy=False)
 
 
