@@ -578,6 +578,7 @@ def _c5_multiturn(args, u, W, torch, ctx, stream, model, ring, params, vals, rng
     wall_mt = time.perf_counter() - t0
     dev_mt = eng.device_ms
     launches += eng.launches
+    tape_segments = eng.last_tape_segments
     del st
     torch.cuda.empty_cache()
     m = args.c5_fd_params
@@ -632,6 +633,7 @@ def _c5_multiturn(args, u, W, torch, ctx, stream, model, ring, params, vals, rng
         'particles': Np, 'turns': T, 'checkpoint_every': ck,
         'regular_particles': int(obj.sum()),
         'regularity': 'final-state growth of a 1e-9 m start displacement < 200x',
+        'tape_segments_in_parallel': tape_segments,
         'adjoint_device_ms': dev_mt, 'adjoint_wall_s': wall_mt,
         'fd_sample_params': m, 'fd_sample_device_ms': dev_fdm,
         'fd_all_params_device_ms_scaled': fd_full,

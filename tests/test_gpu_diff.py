@@ -251,3 +251,21 @@ def test_segment_grouping_is_bit_identical():
     assert [r[2] for r in out] == [1, 2, 6]
     for zb, pb, _ in out[1:]:
         assert np.array_equal(zb, out[0][0]) and np.array_equal(pb, out[0][1])
+
+
+def test_pair_lane_forward_is_bit_identical_to_one_lane():
+    """Plain mode runs each job on two lanes (x and y planes) with the same
+    IEEE operations in the same order as the one-lane tangent-mode code: the
+    states must agree bit for bit (checkpointed, 37 jobs so warps are ragged)."""
+    import ufo_gb300 as u
+    from ufo_gb300 import diff as D, workloads as W
+    ring = _ring()
+    params, vals = _params(ring)
+    rows = vals[None] * (1 + 1e-3 * np.random.default_rng(2).standard_normal((2, len(vals))))
+    eng = D.DiffEngine(D.DiffProgram(ring, u.KICK, params, rows))
+    c = W.c2_beam(37, seed=8)
+    o = 1 / (1 + c[:, 5])
+    seed = (np.arange(37) % 2).astype(np.int32)
+    plain, _ = eng.forward(c[:, :4], o, 7, ck=3, seed=seed)
+    tang, _ = eng.forward(c[:, :4], o, 7, tangent=True, ck=3, seed=seed)
+    assert np.array_equal(plain[:, :4], tang[:, :4])

@@ -131,8 +131,8 @@ __device__ __forceinline__ void fwd_kick(St &s, const double *a, int M, double o
   } else {
     series<0>(a, M, s.x, s.y, sr, si, ar, ai, br, bi);
   }
-  s.px -= o * sr;
-  s.py += o * si;
+  s.px = fma(-o, sr, s.px);
+  s.py = fma(o, si, s.py);
 }
 
 // tape slot of field f of kick k in turn tt (counted from the start of the
@@ -146,25 +146,12 @@ __device__ __forceinline__ int64_t tidx(const DiffArgs &a, int tt, int k, int f,
              TLANES + (j % TLANES);
 }
 
-// forward kick that also records x, y and S'(z) on the rich tape
-__device__ __forceinline__ void fwd_kick_rich(St &s, const double *a, int M, double o, double *t0,
-                                              int64_t stride) {
-  double sr, si, ar, ai, br, bi;
-  series<1>(a, M, s.x, s.y, sr, si, ar, ai, br, bi);
-  t0[0] = s.x;
-  t0[stride] = s.y;
-  t0[2 * stride] = o * ar;
-  t0[3 * stride] = o * ai;
-  s.px -= o * sr;
-  s.py += o * si;
-}
-
-// one turn forward; with `tape` the state at every kick is recorded as turn
-// `tt` of the group (tangent: x, y and the x/y rows of T; plain: x, y, S'/o)
+// one turn forward (one lane per job); with `tape` (tangent mode) x, y and
+// the x/y rows of T at every kick are recorded as turn `tt`
 __device__ void turn_forward(St &s, const DiffArgs &a, const double *T0, double o, bool tangent,
                              int j, int tt, bool tape) {
   int kidx = 0;
-  const int nf = tangent ? 10 : 4;
+  const int nf = 10;
   for (int i = 0; i < a.n_ops; ++i) {
     const DOp op = a.ops[i];
     const double *c = T0 + op.toff;
@@ -198,13 +185,7 @@ __device__ void turn_forward(St &s, const DiffArgs &a, const double *T0, double 
         if (tp) fwd_drift(s, Lo, tangent);
         for (int sl = 0; sl < N; ++sl) {
           const int k = kidx++;
-          if (tape && !tangent) {
-            fwd_kick_rich(s, c + KHDR, op.M, oo, a.tape + tidx(a, tt, k, 0, nf, j), TLANES);
-            if (tp && W != 0.0) fwd_weak(s, W, tangent);
-            if (tp) fwd_drift(s, sl < N - 1 ? Li : Lo, tangent);
-            continue;
-          }
-          if (tape) {
+          if (tape) {  // tangent tape (the plain rich tape is written by the pair kernels)
             double *t = a.tape;
             t[tidx(a, tt, k, 0, nf, j)] = s.x;
             t[tidx(a, tt, k, 1, nf, j)] = s.y;
@@ -377,21 +358,6 @@ __device__ __forceinline__ void zpow_small(double x, double y, int pm, double &z
   }
 }
 
-// reverse of one plain kick from the rich tape (x, y, S'): no polynomial
-// evaluation; adds the parameter cotangent of weight z^pm / o to g0
-__device__ __forceinline__ void rev_kick_rich(Bar &b, const double *t0, int64_t stride, int pm,
-                                              double &g0) {
-  const double a1 = t0[2 * stride], b1 = t0[3 * stride];
-  const double pxb = b.px, pyb = b.py;
-  b.x = fma(-pxb, a1, fma(pyb, b1, b.x));
-  b.y = fma(pxb, b1, fma(pyb, a1, b.y));
-  if (pm >= 0) {
-    double zr, zi;
-    zpow_small(t0[0], t0[stride], pm, zr, zi);
-    g0 = fma(-pxb, zr, fma(pyb, zi, g0));
-  }
-}
-
 // The reverse walk reads the tape backwards from HBM with one warp per SM,
 // one dependent access per kick.  Lane 0 asks the copy engine to bring the
 // warp's next chunks (CHUNK kicks, 64 KiB) into L2 ahead of use: fire and
@@ -409,58 +375,6 @@ __device__ __forceinline__ void prefetch_chunk(const DiffArgs &a, int tt, int k0
   if (hi <= lo || (j % TLANES) != 0) return;
   prefetch_l2_bulk(a.tape + tidx(a, tt, lo, 0, 4, j),
                    static_cast<uint32_t>((hi - lo) * 4 * TLANES * sizeof(double)));
-}
-
-// reverse of turn `tt` of the group from the rich tape (plain mode)
-__device__ void turn_reverse_plain(Bar &b, const DiffArgs &a, const double *T0, double o, int j,
-                                   int tt) {
-  int kidx = a.kicks_per_turn;
-  // the first two chunks of this turn's walk (its last kicks)
-  const int top = ((a.kicks_per_turn - 1) / CHUNK) * CHUNK;
-  prefetch_chunk(a, tt, top, j);
-  prefetch_chunk(a, tt, top - CHUNK, j);
-  for (int i = a.n_ops - 1; i >= 0; --i) {
-    const DOp op = a.ops[i];
-    const double *c = T0 + op.toff;
-    const double oo = op.achro ? 1.0 : o;
-    switch (op.kind) {
-      case D_DRIFT:
-        rev_drift(b, __ldg(c), false);
-        break;
-      case D_ALIGN:
-        break;
-      case D_EDGE: {
-        const double curv = __ldg(c) * oo;
-        b.x = fma(b.px * curv, __ldg(c + 1), b.x);
-        b.y = fma(-(b.py * curv), __ldg(c + 2), b.y);
-        break;
-      }
-      case D_KICK:
-      case D_TEAPOT: {
-        const bool tp = op.kind == D_TEAPOT;
-        const int N = tp ? op.N : 1;
-        const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2);
-        const int pm = op.pslot >= 0 ? op.pm : -1;
-        double g0 = 0.0;
-        for (int sl = N - 1; sl >= 0; --sl) {
-          if (tp) rev_drift(b, sl < N - 1 ? Li : Lo, false);
-          if (tp && W != 0.0) rev_weak(b, W, false);
-          --kidx;
-          if (kidx % CHUNK == 0 && kidx >= 2 * CHUNK)  // entering a chunk: two ahead
-            prefetch_chunk(a, tt, kidx - 2 * CHUNK, j);
-          rev_kick_rich(b, a.tape + tidx(a, tt, kidx, 0, 4, j), TLANES, pm, g0);
-        }
-        if (tp) rev_drift(b, Lo, false);
-        if (op.pslot >= 0) {  // dS/dc = o z^pm / pm!
-          double &p = a.pbar[static_cast<int64_t>(op.pslot) * a.n_jobs + j];
-          p = fma(g0 * oo, __ldg(c + 3), p);
-        }
-        break;
-      }
-      default:
-        break;
-    }
-  }
 }
 
 __device__ void save_ckpt(const St &s, const DiffArgs &a, int c, int j, bool tangent) {
@@ -531,42 +445,364 @@ __global__ void diff_reverse(DiffArgs a) {
   a.zbar0[4 * j + 3] = b.py;
 }
 
-// plain mode, step 1: G segments [sg0, sg0 + G) re-tracked from their
-// checkpoints onto the rich tape, one thread per (segment, job), jobs fastest
-__global__ void diff_tape(DiffArgs a, int sg0, int G) {
-  const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-  if (t >= static_cast<int64_t>(G) * a.n_jobs) return;
-  const int g = static_cast<int>(t / a.n_jobs), j = static_cast<int>(t % a.n_jobs);
-  const int sg = sg0 + g;
-  const int t0 = sg * a.ck;
-  if (t0 >= a.turns) return;
-  const int t1 = min(a.turns, t0 + a.ck);
-  const double o = a.o[j];
-  const double *T0 = a.tab + (a.seed ? static_cast<int64_t>(a.seed[j]) : 0) * a.tab_stride;
-  St s;
-  load_ckpt(s, a, sg, j, false);
-  for (int tt = t0; tt < t1; ++tt) turn_forward(s, a, T0, o, false, j, g * a.ck + (tt - t0), true);
+// ---------------------------------------------------------------- lane pairs
+// Plain (non-tangent) mode runs every job on two lanes of a warp: the even
+// lane carries the horizontal plane (x, px), the odd lane the vertical one
+// (y, py), so a warp holds 16 jobs and a sweep of J jobs has twice the warps
+// (the SM sub-partitions are what the one-thread-per-job sweep leaves idle).
+// Each quantity is computed by the same IEEE operations, in the same order, as
+// in the one-lane code above; the lanes exchange values by warp shuffles where
+// a quantity needs both planes (z = x + iy of a kick, the complex Horner
+// steps, the momentum cotangents of the reverse kick).  Lanes of a job past
+// the end keep running on a clamped job (every shuffle has all 32 lanes) and
+// write nothing.
+constexpr unsigned ALL_LANES = 0xffffffffu;
+
+struct Half {
+  double u, pu;  // this lane's plane: (x, px) on even lanes, (y, py) on odd lanes
+};
+
+__device__ __forceinline__ double other(double v) { return __shfl_xor_sync(ALL_LANES, v, 1); }
+
+// S(z)/o (and S'(z)/o with ND = 1) split over the pair: `r0` / `r1` are this
+// lane's part (real on even lanes, imaginary on odd lanes)
+template <int ND>
+__device__ __forceinline__ void series_pair(const double *__restrict__ a, int M, double x, double y,
+                                            bool even, double &r0, double &r1) {
+  const double *b = a + M;
+  const double p = even ? x : y, q = even ? y : x;
+  r0 = even ? __ldg(a + M - 1) : __ldg(b + M - 1);
+  r1 = 0.0;
+  for (int n = M - 2; n >= 0; --n) {
+    const double o0 = other(r0);
+    const double sr0 = even ? r0 : o0, si0 = even ? o0 : r0;
+    if (ND >= 1) {
+      const double o1 = other(r1);
+      const double sr1 = even ? r1 : o1, si1 = even ? o1 : r1;
+      // re: fma(s1r, x, fma(-s1i, y, s0r)); im: fma(s1r, y, fma(s1i, x, s0i))
+      r1 = fma(sr1, p, fma(even ? -si1 : si1, q, even ? sr0 : si0));
+    }
+    const double c = even ? __ldg(a + n) : __ldg(b + n);
+    r0 = fma(sr0, p, fma(even ? -si0 : si0, q, c));
+  }
 }
 
-// plain mode, step 2: the segments [sg0, sg_hi] reversed from the tape, one
-// thread per job; the cotangent of the state is read from and written back to
-// zbar0
-__global__ void diff_reverse_plain(DiffArgs a, int sg0, int sg_hi) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= a.n_jobs) return;
+// a kick element of the pair with its M coefficients (this lane's part: the
+// normal list on even lanes, the skew list on odd lanes) loaded into
+// registers once for all N slices; the unrolled Horner issues no loads
+template <int M>
+__device__ __forceinline__ void kick_elem_pair(Half &h, const DiffArgs &a, const double *c, bool tp,
+                                               int N, double oo, bool even, int j, bool write,
+                                               int tt, bool tape, int &kidx) {
+  double cf[M];
+  const double *src = c + KHDR + (even ? 0 : M);
+#pragma unroll
+  for (int n = 0; n < M; ++n) cf[n] = __ldg(src + n);
+  const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2);
+  if (tp) h.u = fma(h.pu, Lo, h.u);
+  for (int sl = 0; sl < N; ++sl) {
+    const int k = kidx++;
+    const double w = other(h.u);
+    const double x = even ? h.u : w, y = even ? w : h.u;
+    const double p = even ? x : y, q = even ? y : x;
+    double r0 = cf[M - 1], r1 = 0.0;
+    if (tape) {
+#pragma unroll
+      for (int n = M - 2; n >= 0; --n) {
+        const double o0 = other(r0), o1 = other(r1);
+        const double sr0 = even ? r0 : o0, si0 = even ? o0 : r0;
+        const double sr1 = even ? r1 : o1, si1 = even ? o1 : r1;
+        r1 = fma(sr1, p, fma(even ? -si1 : si1, q, even ? sr0 : si0));
+        r0 = fma(sr0, p, fma(even ? -si0 : si0, q, cf[n]));
+      }
+      if (write) {
+        double *t0 = a.tape + tidx(a, tt, k, 0, 4, j);
+        t0[even ? 0 : TLANES] = h.u;
+        t0[(even ? 2 : 3) * TLANES] = oo * r1;
+      }
+    } else {
+#pragma unroll
+      for (int n = M - 2; n >= 0; --n) {
+        const double o0 = other(r0);
+        const double sr0 = even ? r0 : o0, si0 = even ? o0 : r0;
+        r0 = fma(sr0, p, fma(even ? -si0 : si0, q, cf[n]));
+      }
+    }
+    h.pu = fma(even ? -oo : oo, r0, h.pu);
+    if (tp && W != 0.0 && even) h.pu = fma(-W, h.u, h.pu);
+    if (tp) h.u = fma(h.pu, sl < N - 1 ? Li : Lo, h.u);
+  }
+}
+
+// one turn forward of the pair; with `tape` the rich tape is written as turn
+// `tt` of the group (x, Re S' by the even lane; y, Im S' by the odd lane)
+__device__ void turn_forward_pair(Half &h, const DiffArgs &a, const double *T0, double o,
+                                  bool even, int j, bool write, int tt, bool tape) {
+  int kidx = 0;
+  for (int i = 0; i < a.n_ops; ++i) {
+    const DOp op = a.ops[i];
+    const double *c = T0 + op.toff;
+    const double oo = op.achro ? 1.0 : o;
+    switch (op.kind) {
+      case D_DRIFT:
+        h.u = fma(h.pu, __ldg(c), h.u);
+        break;
+      case D_ALIGN:
+        h.u -= __ldg(c + (even ? 0 : 1));
+        break;
+      case D_EDGE: {
+        const double curv = __ldg(c) * oo;
+        const double t = h.u * curv;
+        h.pu = fma(even ? t : -t, __ldg(c + (even ? 1 : 2)), h.pu);
+        break;
+      }
+      case D_KICK:
+      case D_TEAPOT: {
+        const bool tp = op.kind == D_TEAPOT;
+        const int N = tp ? op.N : 1;
+        switch (op.M) {  // common orders: coefficients in registers
+          case 1: kick_elem_pair<1>(h, a, c, tp, N, oo, even, j, write, tt, tape, kidx); continue;
+          case 2: kick_elem_pair<2>(h, a, c, tp, N, oo, even, j, write, tt, tape, kidx); continue;
+          case 3: kick_elem_pair<3>(h, a, c, tp, N, oo, even, j, write, tt, tape, kidx); continue;
+          case 4: kick_elem_pair<4>(h, a, c, tp, N, oo, even, j, write, tt, tape, kidx); continue;
+          case 5: kick_elem_pair<5>(h, a, c, tp, N, oo, even, j, write, tt, tape, kidx); continue;
+          case 6: kick_elem_pair<6>(h, a, c, tp, N, oo, even, j, write, tt, tape, kidx); continue;
+          case 7: kick_elem_pair<7>(h, a, c, tp, N, oo, even, j, write, tt, tape, kidx); continue;
+          case 8: kick_elem_pair<8>(h, a, c, tp, N, oo, even, j, write, tt, tape, kidx); continue;
+          default: break;
+        }
+        const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2);
+        if (tp) h.u = fma(h.pu, Lo, h.u);
+        for (int sl = 0; sl < N; ++sl) {
+          const int k = kidx++;
+          const double w = other(h.u);
+          const double x = even ? h.u : w, y = even ? w : h.u;
+          double s0, s1;
+          if (tape) {
+            series_pair<1>(c + KHDR, op.M, x, y, even, s0, s1);
+            if (write) {
+              double *t0 = a.tape + tidx(a, tt, k, 0, 4, j);
+              t0[even ? 0 : TLANES] = h.u;
+              t0[(even ? 2 : 3) * TLANES] = oo * s1;
+            }
+          } else {
+            series_pair<0>(c + KHDR, op.M, x, y, even, s0, s1);
+          }
+          h.pu = fma(even ? -oo : oo, s0, h.pu);
+          if (tp && W != 0.0 && even) h.pu = fma(-W, h.u, h.pu);
+          if (tp) h.u = fma(h.pu, sl < N - 1 ? Li : Lo, h.u);
+        }
+        break;
+      }
+      default:
+        break;
+    }
+  }
+}
+
+// reverse of a kick element of the pair with the tape values of its N slices
+// (x, y, Re S', Im S') loaded up front, before the dependent cotangent chain
+template <int N>
+__device__ __forceinline__ void rev_elem_pair(Half &bh, const DiffArgs &a, const double *c, bool tp,
+                                              double oo, bool even, int j, bool write, int tt,
+                                              int pm, int &kidx, double &g0) {
+  double tx[N], ty[N], ta[N], tb[N];
+#pragma unroll
+  for (int q = 0; q < N; ++q) {
+    const double *t0 = a.tape + tidx(a, tt, kidx - 1 - q, 0, 4, j);
+    tx[q] = t0[0];
+    ty[q] = t0[TLANES];
+    ta[q] = t0[2 * TLANES];
+    tb[q] = t0[3 * TLANES];
+  }
+  const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2);
+#pragma unroll
+  for (int q = 0; q < N; ++q) {  // slice N-1-q
+    if (tp) bh.pu = fma(bh.u, q > 0 ? Li : Lo, bh.pu);
+    if (tp && W != 0.0 && even) bh.u = fma(-W, bh.pu, bh.u);
+    --kidx;
+    if (write && even && kidx % CHUNK == 0 && kidx >= 2 * CHUNK)
+      prefetch_chunk(a, tt, kidx - 2 * CHUNK, j);
+    const double a1 = ta[q], b1 = tb[q];
+    const double w = other(bh.pu);
+    const double pxb = even ? bh.pu : w, pyb = even ? w : bh.pu;
+    bh.u = fma(even ? -pxb : pxb, even ? a1 : b1, fma(pyb, even ? b1 : a1, bh.u));
+    if (pm >= 0) {
+      double zr, zi;
+      zpow_small(tx[q], ty[q], pm, zr, zi);
+      g0 = fma(-pxb, zr, fma(pyb, zi, g0));
+    }
+  }
+  if (tp) bh.pu = fma(bh.u, Lo, bh.pu);
+}
+
+// reverse of turn `tt` of the group from the rich tape, split over the pair
+// (cotangents of x, px on even lanes, of y, py on odd lanes)
+__device__ void turn_reverse_pair(Half &bh, const DiffArgs &a, const double *T0, double o,
+                                  bool even, int j, bool write, int tt) {
+  int kidx = a.kicks_per_turn;
+  const int top = ((a.kicks_per_turn - 1) / CHUNK) * CHUNK;
+  if (write && even) {
+    prefetch_chunk(a, tt, top, j);
+    prefetch_chunk(a, tt, top - CHUNK, j);
+  }
+  for (int i = a.n_ops - 1; i >= 0; --i) {
+    const DOp op = a.ops[i];
+    const double *c = T0 + op.toff;
+    const double oo = op.achro ? 1.0 : o;
+    switch (op.kind) {
+      case D_DRIFT:
+        bh.pu = fma(bh.u, __ldg(c), bh.pu);
+        break;
+      case D_ALIGN:
+        break;
+      case D_EDGE: {
+        const double curv = __ldg(c) * oo;
+        const double t = bh.pu * curv;
+        bh.u = fma(even ? t : -t, __ldg(c + (even ? 1 : 2)), bh.u);
+        break;
+      }
+      case D_KICK:
+      case D_TEAPOT: {
+        const bool tp = op.kind == D_TEAPOT;
+        const int N = tp ? op.N : 1;
+        const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2);
+        const int pm = op.pslot >= 0 ? op.pm : -1;
+        double g0 = 0.0;
+        bool done = true;
+        switch (N) {  // common slice counts: the element's tape values up front
+          case 1: rev_elem_pair<1>(bh, a, c, tp, oo, even, j, write, tt, pm, kidx, g0); break;
+          case 2: rev_elem_pair<2>(bh, a, c, tp, oo, even, j, write, tt, pm, kidx, g0); break;
+          case 4: rev_elem_pair<4>(bh, a, c, tp, oo, even, j, write, tt, pm, kidx, g0); break;
+          case 8: rev_elem_pair<8>(bh, a, c, tp, oo, even, j, write, tt, pm, kidx, g0); break;
+          default: done = false; break;
+        }
+        for (int sl = N - 1; !done && sl >= 0; --sl) {
+          if (tp) bh.pu = fma(bh.u, sl < N - 1 ? Li : Lo, bh.pu);
+          if (tp && W != 0.0 && even) bh.u = fma(-W, bh.pu, bh.u);
+          --kidx;
+          if (write && even && kidx % CHUNK == 0 && kidx >= 2 * CHUNK)
+            prefetch_chunk(a, tt, kidx - 2 * CHUNK, j);
+          const double *t0 = a.tape + tidx(a, tt, kidx, 0, 4, j);
+          const double a1 = t0[2 * TLANES], b1 = t0[3 * TLANES];
+          const double w = other(bh.pu);
+          const double pxb = even ? bh.pu : w, pyb = even ? w : bh.pu;
+          // x: fma(-pxb, a1, fma(pyb, b1, xb)); y: fma(pxb, b1, fma(pyb, a1, yb))
+          bh.u = fma(even ? -pxb : pxb, even ? a1 : b1, fma(pyb, even ? b1 : a1, bh.u));
+          if (pm >= 0) {
+            double zr, zi;
+            zpow_small(t0[0], t0[TLANES], pm, zr, zi);
+            g0 = fma(-pxb, zr, fma(pyb, zi, g0));
+          }
+        }
+        if (tp && !done) bh.pu = fma(bh.u, Lo, bh.pu);
+        if (op.pslot >= 0 && write && even) {
+          double &p = a.pbar[static_cast<int64_t>(op.pslot) * a.n_jobs + j];
+          p = fma(g0 * oo, __ldg(c + 3), p);
+        }
+        break;
+      }
+      default:
+        break;
+    }
+  }
+}
+
+// pair index of this thread: job j (clamped), lane parity, whether it writes
+__device__ __forceinline__ void pair_of(int64_t t, int64_t jobs, int64_t &job, bool &even,
+                                        bool &write) {
+  job = t >> 1;
+  even = (t & 1) == 0;
+  write = job < jobs;
+  if (!write) job = jobs - 1;
+}
+
+__global__ void diff_forward_pair(DiffArgs a) {
+  const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if ((t & ~static_cast<int64_t>(31)) >= 2 * static_cast<int64_t>(a.n_jobs)) return;  // whole warp past the end
+  int64_t jl;
+  bool even, write;
+  pair_of(t, a.n_jobs, jl, even, write);
+  const int j = static_cast<int>(jl);
+  Half h;
+  h.u = a.z0[4 * j + (even ? 0 : 2)];
+  h.pu = a.z0[4 * j + (even ? 1 : 3)];
   const double o = a.o[j];
   const double *T0 = a.tab + (a.seed ? static_cast<int64_t>(a.seed[j]) : 0) * a.tab_stride;
-  Bar b;
-  b.x = a.zbar0[4 * j]; b.px = a.zbar0[4 * j + 1]; b.y = a.zbar0[4 * j + 2];
-  b.py = a.zbar0[4 * j + 3];
+  const bool ck = a.ckpt != nullptr;
+  const int f0 = even ? 0 : 2;
+  for (int tt = 0; tt < a.turns; ++tt) {
+    if (ck && tt % a.ck == 0 && write) {
+      double *d = a.ckpt + static_cast<int64_t>(tt / a.ck) * 20 * a.n_jobs + j;
+      d[f0 * static_cast<int64_t>(a.n_jobs)] = h.u;
+      d[(f0 + 1) * static_cast<int64_t>(a.n_jobs)] = h.pu;
+    }
+    turn_forward_pair(h, a, T0, o, even, j, write, 0, false);
+  }
+  if (write) {
+    if (ck && a.turns % a.ck == 0) {
+      double *d = a.ckpt + static_cast<int64_t>(a.turns / a.ck) * 20 * a.n_jobs + j;
+      d[f0 * static_cast<int64_t>(a.n_jobs)] = h.u;
+      d[(f0 + 1) * static_cast<int64_t>(a.n_jobs)] = h.pu;
+    }
+    double *d = a.zT + 20 * static_cast<int64_t>(j);
+    d[f0] = h.u;
+    d[f0 + 1] = h.pu;
+    if (even)
+      for (int k = 4; k < 20; ++k) d[k] = 0.0;
+  }
+}
+
+__global__ void diff_tape_pair(DiffArgs a, int sg0, int G) {
+  const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  const int64_t pairs = static_cast<int64_t>(G) * a.n_jobs;
+  if ((t & ~static_cast<int64_t>(31)) >= 2 * pairs) return;
+  int64_t q;
+  bool even, write;
+  pair_of(t, pairs, q, even, write);
+  const int g = static_cast<int>(q / a.n_jobs), j = static_cast<int>(q % a.n_jobs);
+  const int sg = sg0 + g;
+  const int t0 = sg * a.ck;
+  const bool live = t0 < a.turns;  // uniform per segment: whole warps agree unless G spans
+  const int t1 = live ? min(a.turns, t0 + a.ck) : t0;
+  const double o = a.o[j];
+  const double *T0 = a.tab + (a.seed ? static_cast<int64_t>(a.seed[j]) : 0) * a.tab_stride;
+  Half h;
+  const int f0 = even ? 0 : 2;
+  const int sl = live ? sg : 0;
+  const double *d = a.ckpt + static_cast<int64_t>(sl) * 20 * a.n_jobs + j;
+  h.u = d[f0 * static_cast<int64_t>(a.n_jobs)];
+  h.pu = d[(f0 + 1) * static_cast<int64_t>(a.n_jobs)];
+  // a warp may straddle two segments (J not a multiple of 16): every lane runs
+  // the longer count; lanes past their own segment end do not write
+  const int tmax = __reduce_max_sync(ALL_LANES, t1 - t0);
+  for (int k = 0; k < tmax; ++k)
+    turn_forward_pair(h, a, T0, o, even, j, write && k < t1 - t0, g * a.ck + k, true);
+}
+
+__global__ void diff_reverse_plain_pair(DiffArgs a, int sg0, int sg_hi) {
+  const int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  if ((t & ~static_cast<int64_t>(31)) >= 2 * static_cast<int64_t>(a.n_jobs)) return;
+  int64_t jl;
+  bool even, write;
+  pair_of(t, a.n_jobs, jl, even, write);
+  const int j = static_cast<int>(jl);
+  const double o = a.o[j];
+  const double *T0 = a.tab + (a.seed ? static_cast<int64_t>(a.seed[j]) : 0) * a.tab_stride;
+  const int f0 = even ? 0 : 2;
+  Half bh;
+  bh.u = a.zbar0[4 * j + f0];
+  bh.pu = a.zbar0[4 * j + f0 + 1];
   for (int sg = sg_hi; sg >= sg0; --sg) {
     const int t0 = sg * a.ck;
     const int t1 = min(a.turns, t0 + a.ck);
     for (int tt = t1 - 1; tt >= t0; --tt)
-      turn_reverse_plain(b, a, T0, o, j, (sg - sg0) * a.ck + (tt - t0));
+      turn_reverse_pair(bh, a, T0, o, even, j, write, (sg - sg0) * a.ck + (tt - t0));
   }
-  a.zbar0[4 * j] = b.x; a.zbar0[4 * j + 1] = b.px; a.zbar0[4 * j + 2] = b.y;
-  a.zbar0[4 * j + 3] = b.py;
+  if (write) {
+    a.zbar0[4 * j + f0] = bh.u;
+    a.zbar0[4 * j + f0 + 1] = bh.pu;
+  }
 }
 
 }  // namespace ufo_diff
@@ -585,8 +821,10 @@ static void prefer_l1() {
   if (done) return;
   cudaFuncSetAttribute(ufo_diff::diff_forward, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
   cudaFuncSetAttribute(ufo_diff::diff_reverse, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
-  cudaFuncSetAttribute(ufo_diff::diff_tape, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
-  cudaFuncSetAttribute(ufo_diff::diff_reverse_plain,
+  cudaFuncSetAttribute(ufo_diff::diff_forward_pair,
+                       cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+  cudaFuncSetAttribute(ufo_diff::diff_tape_pair, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+  cudaFuncSetAttribute(ufo_diff::diff_reverse_plain_pair,
                        cudaFuncAttributePreferredSharedMemoryCarveout, 0);
   done = true;
 }
@@ -615,7 +853,13 @@ int ufo_diff_forward(const int32_t *ops, int n_ops, const double *tab, int64_t t
   a.ckpt = ckpt;
   a.zT = zT;
   const int tpb = 32;
-  ufo_diff::diff_forward<<<(n_jobs + tpb - 1) / tpb, tpb, 0, static_cast<cudaStream_t>(stream)>>>(a);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (tangent) {
+    ufo_diff::diff_forward<<<(n_jobs + tpb - 1) / tpb, tpb, 0, st>>>(a);
+  } else {  // two lanes per job
+    const int64_t threads = 2 * static_cast<int64_t>(n_jobs);
+    ufo_diff::diff_forward_pair<<<static_cast<unsigned>((threads + tpb - 1) / tpb), tpb, 0, st>>>(a);
+  }
   return cudaGetLastError() == cudaSuccess ? 0 : -2;
 }
 
@@ -666,9 +910,12 @@ int ufo_diff_reverse(const int32_t *ops, int n_ops, const double *tab, int64_t t
   for (int hi = last_seg; hi >= 0; hi -= tape_segments) {
     const int lo = hi - tape_segments + 1 < 0 ? 0 : hi - tape_segments + 1;
     const int G = hi - lo + 1;
-    const int64_t threads = static_cast<int64_t>(G) * n_jobs;
-    ufo_diff::diff_tape<<<static_cast<unsigned>((threads + tpb - 1) / tpb), tpb, 0, st>>>(a, lo, G);
-    ufo_diff::diff_reverse_plain<<<(n_jobs + tpb - 1) / tpb, tpb, 0, st>>>(a, lo, hi);
+    const int64_t threads = 2 * static_cast<int64_t>(G) * n_jobs;  // two lanes per job
+    ufo_diff::diff_tape_pair<<<static_cast<unsigned>((threads + tpb - 1) / tpb), tpb, 0, st>>>(
+        a, lo, G);
+    const int64_t rthreads = 2 * static_cast<int64_t>(n_jobs);
+    ufo_diff::diff_reverse_plain_pair<<<static_cast<unsigned>((rthreads + tpb - 1) / tpb), tpb, 0,
+                                        st>>>(a, lo, hi);
     if (cudaGetLastError() != cudaSuccess) return -2;
   }
   return 0;

@@ -265,6 +265,7 @@ class DiffEngine:
         n_seg = (turns - 1) // ck + 1
         budget = self.tape_budget
         if budget is None:
+            torch.cuda.empty_cache()  # cached but unused blocks count as free here
             free, _ = torch.cuda.mem_get_info(self.dev)
             budget = min(128 << 30, int(0.4 * free))
         G = 1 if tangent else int(max(1, min(n_seg, budget // max(1, seg_bytes))))
