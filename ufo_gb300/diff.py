@@ -268,7 +268,19 @@ class DiffEngine:
             torch.cuda.empty_cache()  # cached but unused blocks count as free here
             free, _ = torch.cuda.mem_get_info(self.dev)
             budget = min(128 << 30, int(0.4 * free))
-        G = 1 if tangent else int(max(1, min(n_seg, budget // max(1, seg_bytes))))
+        if tangent:
+            G = 1
+        else:
+            # segments taped at once: bounded by memory and by parallelism (the
+            # taping pass runs two lanes per job; about 1.5 warps per SM
+            # sub-partition fill the GPU, more only queue), then balanced so
+            # the groups are equal
+            smsp = 4 * torch.cuda.get_device_properties(self.dev).multi_processor_count
+            warps_per_seg = -(-2 * J // 32)
+            g_par = max(1, round(1.5 * smsp / warps_per_seg))
+            G = int(max(1, min(n_seg, budget // max(1, seg_bytes), g_par)))
+            groups = -(-n_seg // G)
+            G = -(-n_seg // groups)
         tape = torch.empty((G * seg_len, W, max(1, self.p.kicks_per_turn), nf, 32),
                            dtype=torch.float64, device=self.dev)
         self.last_tape_segments = G
