@@ -273,6 +273,16 @@ UFO_DEV void horner_trim(const State &s, int n, uint32_t mask, const double *c, 
 
 struct PxPy { double px, py; };
 
+// FMA mode, sextupole kick with t = (K*o)/2 and t2 = 2t = K*o:
+//   px -= t (x^2 - y^2),  py += t2 x y
+// 2 DMUL + 3 DFMA instead of the reference's form's 2 DMUL + 4 DFMA
+UFO_DEV void sext_fma(State &s, double t, double t2) {
+  const double d = fma_(s.x, s.x, -mul(s.y, s.y));
+  const double xy = mul(s.x, s.y);
+  s.px = fma_(-t, d, s.px);
+  s.py = fma_(t2, xy, s.py);
+}
+
 // FMA mode, general multipole.  The reference's kick (ufo/methods.py:45-76)
 // runs one real Horner pass for the normal and one for the skew list, dividing
 // by the order at every step; both are the one complex polynomial
@@ -367,11 +377,10 @@ UFO_DEV void kick(State &s, int nn, int ns, uint32_t mn, uint32_t ms, const doub
     } else if (nn == 3 && mn == 4u) {
       // sextupole: a = ((K*o)*x)/2 = ((K*o)*0.5)*x exactly (power-of-two scaling)
       const double t = mul(achro ? ld(c) : mul(ld(c), s.o), 0.5);
-      const double a = mul(t, s.x), b = mul(t, s.y);
       if (FMA) {
-        s.px = fma_(b, s.y, fma_(-a, s.x, s.px));
-        s.py = fma_(b, s.x, fma_(a, s.y, s.py));
+        sext_fma(s, t, add(t, t));
       } else {
+        const double a = mul(t, s.x), b = mul(t, s.y);
         s.px = sub(s.px, sub(mul(a, s.x), mul(b, s.y)));
         s.py = add(s.py, add(mul(a, s.y), mul(b, s.x)));
       }
@@ -463,7 +472,7 @@ __device__ __noinline__ PxPy slow_slice(double x, double y, double px, double py
 
 template <bool FMA, int PAT, bool WEAK>
 UFO_DEV void tp_slice(State &s, int nn, int ns, uint32_t mn, uint32_t ms, const double *ck,
-                      bool achro, double t, double W) {
+                      bool achro, double t, double t2, double W) {
   if (s.bad_o || nf(s.x) || nf(s.y)) {
     const PxPy r = slow_slice<FMA>(s.x, s.y, s.px, s.py, s.o, s.bad_o, nn, ns, mn, ms, ck, achro,
                                    WEAK, W);
@@ -489,11 +498,10 @@ UFO_DEV void tp_slice(State &s, int nn, int ns, uint32_t mn, uint32_t ms, const 
       s.py = add(s.py, mul(t, s.y));
     }
   } else if (PAT == 2) {
-    const double a = mul(t, s.x), b = mul(t, s.y);
     if (FMA) {
-      s.px = fma_(b, s.y, fma_(-a, s.x, s.px));
-      s.py = fma_(b, s.x, fma_(a, s.y, s.py));
+      sext_fma(s, t, t2);
     } else {
+      const double a = mul(t, s.x), b = mul(t, s.y);
       s.px = sub(s.px, sub(mul(a, s.x), mul(b, s.y)));
       s.py = add(s.py, add(mul(a, s.y), mul(b, s.x)));
     }
@@ -511,19 +519,20 @@ UFO_DEV void teapot_v(State &s, const Op &op, const double *c) {
   const double *ck = ci + (N > 1 ? (DIVIN ? 4 : 1) : 0);
   const double W = WEAK ? ld(ck + __popc(mn) + __popc(ms)) : 0.0;
   const double o1 = achro ? 1.0 : s.o;
-  double t = 0.0;
+  double t = 0.0, t2 = 0.0;
   if (PAT == 1) t = mul(ld(ck), o1);
   if (PAT == 2) t = mul(mul(ld(ck), o1), 0.5);
+  if (FMA && PAT == 2) t2 = add(t, t);
   const double Li = DIVIN ? 0.0 : ld(ci);
   drift_L<FMA>(s, Lo);
   for (int sl = 1; sl < N; ++sl) {
-    tp_slice<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, t, W);
+    tp_slice<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, t, t2, W);
     if (DIVIN)
       drift_div<FMA>(s, ci);
     else
       drift_L<FMA>(s, Li);
   }
-  tp_slice<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, t, W);
+  tp_slice<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, t, t2, W);
   drift_L<FMA>(s, Lo);
 }
 
@@ -538,7 +547,7 @@ UFO_DEV void teapot_v(State &s, const Op &op, const double *c) {
 // strengths of the quadrupole/sextupole patterns are formed once per element.
 template <bool FMA, int PAT, bool WEAK>
 UFO_DEV void y_kick(State &s, int nn, int ns, uint32_t mn, uint32_t ms, const double *ck,
-                    bool achro, double w, double t, double Ww) {
+                    bool achro, double w, double t, double t2, double Ww) {
   if (PAT == 0 && FMA && (mn | ms) != 0u) {
     kick_cplx(s, mn, ms, ck, achro, w);
   } else if (PAT == 0) {
@@ -561,11 +570,10 @@ UFO_DEV void y_kick(State &s, int nn, int ns, uint32_t mn, uint32_t ms, const do
       s.py = add(s.py, mul(t, s.y));
     }
   } else if (PAT == 2) {
-    const double a = mul(t, s.x), b = mul(t, s.y);
     if (FMA) {
-      s.px = fma_(b, s.y, fma_(-a, s.x, s.px));
-      s.py = fma_(b, s.x, fma_(a, s.y, s.py));
+      sext_fma(s, t, t2);
     } else {
+      const double a = mul(t, s.x), b = mul(t, s.y);
       s.px = sub(s.px, sub(mul(a, s.x), mul(b, s.y)));
       s.py = add(s.py, add(mul(a, s.y), mul(b, s.x)));
     }
@@ -590,6 +598,10 @@ UFO_DEV void yoshida_v(State &s, const Op &op, const double *c) {
     t1 = mul(t, w1);
     t2 = mul(t, w2);
   }
+  // doubled strengths of the FMA sextupole form
+  const double u0 = (FMA && PAT == 2) ? add(t0, t0) : 0.0;
+  const double u1 = (FMA && PAT == 2) ? add(t1, t1) : 0.0;
+  const double u2 = (FMA && PAT == 2) ? add(t2, t2) : 0.0;
   if (WEAK) {
     const double W = ld(ck + __popc(mn) + __popc(ms));
     W0 = mul(W, w0);
@@ -598,11 +610,11 @@ UFO_DEV void yoshida_v(State &s, const Op &op, const double *c) {
   }
   for (int sl = 0; sl < N; ++sl) {
     drift_L<FMA>(s, d0);
-    y_kick<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, w0, t0, W0);
+    y_kick<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, w0, t0, u0, W0);
     drift_L<FMA>(s, d1);
-    y_kick<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, w1, t1, W1);
+    y_kick<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, w1, t1, u1, W1);
     drift_L<FMA>(s, d2);
-    y_kick<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, w2, t2, W2);
+    y_kick<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, w2, t2, u2, W2);
     drift_L<FMA>(s, d3);
   }
 }
