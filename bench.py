@@ -462,9 +462,13 @@ def bench_c3(args):
     tflags = capi.UFO_TRACK_FMA if args.mode == 'fma' else 0
     prog = C.compile_line(ring, flags, where=[-1])
     dprog = capi.DeviceProgram(ctx, prog)
-    perm = np.random.default_rng(3).permutation(n)
-    inputs = {'sorted': torch.from_numpy(grid).to(dev),
-              'shuffled': torch.from_numpy(np.ascontiguousarray(grid[perm])).to(dev)}
+    perms = {'shuffled': np.random.default_rng(3).permutation(n),
+             # largest amplitude first: the early losses churn through the
+             # refill first and the survivors follow as one block
+             'amplitude': np.lexsort((-np.abs(grid[:, 5]), -np.hypot(grid[:, 0], grid[:, 2])))}
+    inputs = {'sorted': torch.from_numpy(grid).to(dev)}
+    for k, pm in perms.items():
+        inputs[k] = torch.from_numpy(np.ascontiguousarray(grid[pm])).to(dev)
     lost = torch.empty(n, dtype=torch.int32, device=dev)
     final = torch.empty((n, 6), dtype=torch.float64, device=dev)
 
@@ -487,16 +491,16 @@ def bench_c3(args):
         e1.record(stream)
         torch.cuda.synchronize()
         lo = lost.cpu().numpy().view(np.uint32).astype(np.int64)
-        if order == 'shuffled':
+        if order in perms:
             un = np.empty_like(lo)
-            un[perm] = lo
+            un[perms[order]] = lo
             lo = un
         return e0.elapsed_time(e1) / steps, ctx.launches() - l0, lo
 
     clocks = Clocks(0)
     clocks.start()
     runs = {}
-    for order in ('sorted', 'shuffled'):
+    for order in ('sorted', 'shuffled', 'amplitude'):
         for plain in (False, True):
             runs[(order, plain)] = timed(order, plain, args.steps if not plain else
                                          max(1, args.steps // 2))
@@ -534,6 +538,10 @@ def bench_c3(args):
                     runs[('shuffled', True)][0] / runs[('shuffled', False)][0],
                 'note': 'the same grid in a seeded random order: warps of the plain '
                         'kernel mix survivors and early losses'},
+            'amplitude_order': {
+                'persistent': pet / (runs[('amplitude', False)][0] / 1e3),
+                'plain': pet / (runs[('amplitude', True)][0] / 1e3),
+                'note': 'the same grid, largest amplitude (then |dp|) first'},
             'identical_loss_turns': bool(all(np.array_equal(lost_p, r[2])
                                              for r in runs.values())),
             'gpu_launches': launches}

@@ -167,6 +167,30 @@ def test_general_kicks_fma_within_tolerance_of_strict(which):
         assert np.array_equal(ls[reg], lf[reg])
 
 
+def test_c3_full_grid_subset_loss_turns_vs_oracle():
+    """The dynamic-aperture benchmark case at full size (C1 ring with apertures
+    and errors, 2,048 turns, StableAperture test): strict-mode loss turns and
+    final coordinates of a random subset of the 196,608 grid particles are the
+    oracle's, bit for bit; the persistent and plain kernels agree on the whole
+    grid."""
+    import ufo_gb300 as u
+    from ufo_gb300 import capi, compiler as C, workloads as W
+    from oracle import oracle as O
+    ring = W.c3_ring(u)
+    grid = W.c3_grid()
+    idx = np.random.default_rng(3).choice(len(grid), 256, replace=False)
+    ctx = u.context(0)
+    dp = capi.DeviceProgram(ctx, C.compile_line(ring, u.KICK, where=[-1]))
+    _, lost, fin = capi.track(ctx, dp, grid[idx], 2048, capi.UFO_MODE_SA, 0, slots=0)
+    ref = O.track(ring, u.KICK, grid[idx], 2048, where=[-1], mode=1, tracks=False)
+    assert np.array_equal(lost, ref['lost'])
+    assert np.array_equal(fin, ref['final'], equal_nan=True)
+    assert 0 < np.sum(lost < 2048) < len(idx)  # survival is uneven
+    _, lp, _ = capi.track(ctx, dp, grid, 2048, capi.UFO_MODE_SA, 0, slots=0)
+    _, lq, _ = capi.track(ctx, dp, grid, 2048, capi.UFO_MODE_SA, capi.UFO_TRACK_PLAIN, slots=0)
+    assert np.array_equal(lp, lq)
+
+
 def test_seed_batch_equals_individual_launches():
     """One launch over many error seeds == one launch per seed, bit for bit."""
     import ufo_gb300 as u
