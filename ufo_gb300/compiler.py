@@ -35,7 +35,7 @@ import numpy as np
 from . import aperture as _ap
 from . import crmath
 from . import elements as E
-from .flags import LINEAR, FIVED, EXACT, KICK, ACHROMATIC, YOSHIDA
+from .flags import LINEAR, FIVED, EXACT, KICK, ACHROMATIC, YOSHIDA, FMA
 
 # ---- opcodes (shared with csrc/ufo_kernels.cuh and oracle) ----
 OP_NOP, OP_DRIFT, OP_KICK, OP_TEAPOT, OP_ALIGN, OP_EDGE, OP_THICKQ, OP_THICKB, OP_WIRE, \
@@ -61,6 +61,7 @@ F_T2Z = 1 << 10         # edge: py term structurally zero (poison-only)
 F_WEAKZ = 1 << 11       # teapot: weak term structurally zero (poison-only)
 F_YOSHIDA = 1 << 12     # teapot: 4th-order Yoshida splitting instead of TEAPOT
 F_CIRCLE = 1 << 13      # aperture: x*x + y*y < c (table: [c])
+F_SPLITO = 1 << 14      # teapot: exit outer drift is its own constant, after the others
 # drift form of teapot outer/inner drifts packed in bits 16..19
 SH_FOUTER, SH_FINNER = 16, 18
 
@@ -807,6 +808,50 @@ def fractures(n, where):
     return per, pre
 
 
+def _merge_drifts(ops):
+    """FMA mode: fold each plain drift (x += px L) into the outer drift of an
+    adjacent non-exact TEAPOT element (x += px (L + Lo)): one op and two FMAs
+    fewer per drift; the sum of lengths changes the rounding only.  A teapot
+    that absorbs a drift after it keeps its exit length as a separate constant
+    (F_SPLITO).  Apertures, edges and observation points stay where they are,
+    so only drifts next to a teapot merge."""
+    def teapot_ok(op):
+        return (op.kind == OP_TEAPOT and not op.flags & (F_EXACT | F_YOSHIDA)
+                and (op.flags >> SH_FOUTER) & 3 == DF_MUL)
+
+    def drift_ok(op):
+        return op.kind == OP_DRIFT and not op.flags & F_EXACT and op.ints[0] == DF_MUL
+
+    out = []
+    i = 0
+    n = len(ops)
+    while i < n:
+        op = ops[i]
+        if drift_ok(op) and i + 1 < n and teapot_ok(ops[i + 1]):
+            t = ops[i + 1]
+            if not t.flags & F_SPLITO:  # the exit keeps the original length
+                t.consts = t.consts + [t.consts[0]]
+                t.flags |= F_SPLITO
+            t.consts[0] = op.consts[0] + t.consts[0]
+            t.flops += op.flops  # the algorithmic count stays the reference's
+            t.flops_fast += op.flops_fast
+            i += 1
+            continue
+        if drift_ok(op) and out and teapot_ok(out[-1]):
+            t = out[-1]
+            if not t.flags & F_SPLITO:
+                t.consts = t.consts + [t.consts[0]]
+                t.flags |= F_SPLITO
+            t.consts[-1] = t.consts[-1] + op.consts[0]
+            t.flops += op.flops
+            t.flops_fast += op.flops_fast
+            i += 1
+            continue
+        out.append(op)
+        i += 1
+    return out
+
+
 def compile_line(line, flags=0, parameters=(), where=(), seed_values=None, count=None,
                  dump_end=None):
     """Compile ``line`` for ``flags``.
@@ -832,6 +877,8 @@ def compile_line(line, flags=0, parameters=(), where=(), seed_values=None, count
             lw.new_segment()
         prm = {name: Val(seed_values[:, col].copy(), False) for name, col in binds[idx].items()}
         lower_element(lw, elem, idx, prm, per[idx])
+    if flags & FMA:
+        lw.segments = [_merge_drifts(seg) for seg in lw.segments]
     if dump_end is None:
         dump_end = -1 in where
     if count is None:

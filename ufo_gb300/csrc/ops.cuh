@@ -23,7 +23,7 @@ enum : int { DF_MUL = 0, DF_MUL2 = 1, DF_DIV = 2 };
 enum : int {
   F_ACHRO = 1 << 0, F_EXACT = 1 << 1, F_WEAK = 1 << 2, F_RTPSI = 1 << 3, F_T1 = 1 << 4,
   F_T2 = 1 << 5, F_CONST = 1 << 6, F_AX = 1 << 7, F_AY = 1 << 8, F_T1Z = 1 << 9,
-  F_T2Z = 1 << 10, F_WEAKZ = 1 << 11, F_YOSHIDA = 1 << 12, F_CIRCLE = 1 << 13
+  F_T2Z = 1 << 10, F_WEAKZ = 1 << 11, F_YOSHIDA = 1 << 12, F_CIRCLE = 1 << 13, F_SPLITO = 1 << 14
 };
 constexpr int SH_FOUTER = 16, SH_FINNER = 18;
 
@@ -533,7 +533,11 @@ UFO_DEV void teapot_v(State &s, const Op &op, const double *c) {
       drift_L<FMA>(s, Li);
   }
   tp_slice<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, t, t2, W);
-  drift_L<FMA>(s, Lo);
+  // exit outer drift: its own constant after the others when a following
+  // drift was merged into it (FMA programs)
+  double Lx = Lo;
+  if (op.flags & F_SPLITO) Lx = ld(ck + __popc(mn) + __popc(ms) + (WEAK ? 1 : 0));
+  drift_L<FMA>(s, Lx);
 }
 
 // ---------------------------------------------------------------- Yoshida

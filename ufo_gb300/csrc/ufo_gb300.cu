@@ -473,7 +473,8 @@ int64_t op_consts(const int32_t *w) {
       const int fo = (flags >> ufo::SH_FOUTER) & 3, fi = (flags >> ufo::SH_FINNER) & 3;
       const int co = drift_consts(fo, exact), ci = w[3] > 1 ? drift_consts(fi, exact) : 0;
       if (co < 0 || ci < 0) return -1;
-      return co + ci + popc32(w[6]) + popc32(w[7]) + ((flags & ufo::F_WEAK) ? 1 : 0);
+      return co + ci + popc32(w[6]) + popc32(w[7]) + ((flags & ufo::F_WEAK) ? 1 : 0) +
+             ((flags & ufo::F_SPLITO) ? 1 : 0);
     }
     case ufo::OP_ALIGN:
       return 2;

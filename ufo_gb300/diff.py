@@ -27,6 +27,7 @@ import math
 import numpy as np
 
 from . import compiler as C
+from .flags import FMA
 
 D_NOP, D_DRIFT, D_TEAPOT, D_KICK, D_ALIGN, D_EDGE = range(6)
 
@@ -49,7 +50,9 @@ class DiffProgram:
             np.atleast_2d(np.asarray(values, np.float64))
         if values is not None and vals.shape[1] != len(parameters):
             vals = vals.reshape(-1, len(parameters))
-        prog = C.compile_line(line, flags, parameters, [], seed_values=vals)
+        # the differentiator has its own arithmetic: compile without FMA-mode
+        # rewrites (merged drifts)
+        prog = C.compile_line(line, flags & ~FMA, parameters, [], seed_values=vals)
         self.prog = prog
         flat = line.flatten() if hasattr(line, 'flatten') else list(line)
         # element index -> (parameter slot, coefficient order)
