@@ -809,12 +809,14 @@ def fractures(n, where):
 
 
 def _merge_drifts(ops):
-    """FMA mode: fold each plain drift (x += px L) into the outer drift of an
-    adjacent non-exact TEAPOT element (x += px (L + Lo)): one op and two FMAs
-    fewer per drift; the sum of lengths changes the rounding only.  A teapot
-    that absorbs a drift after it keeps its exit length as a separate constant
-    (F_SPLITO).  Apertures, edges and observation points stay where they are,
-    so only drifts next to a teapot merge."""
+    """FMA mode: fold each plain drift (x += px L) into the outer drift of a
+    nearby non-exact TEAPOT element (x += px (L + Lo)): one op and two FMAs
+    fewer per drift; the sum of lengths changes the rounding only.  A drift
+    commutes with the alignment shifts between it and the teapot (they move x
+    and y, not px and py), so those may lie in between; apertures, edges and
+    observation points may not.  A teapot that absorbs a drift after it keeps
+    its exit length as a separate constant (F_SPLITO).  Flop counts keep the
+    merged drifts (the algorithmic count is the reference's)."""
     def teapot_ok(op):
         return (op.kind == OP_TEAPOT and not op.flags & (F_EXACT | F_YOSHIDA)
                 and (op.flags >> SH_FOUTER) & 3 == DF_MUL)
@@ -822,31 +824,39 @@ def _merge_drifts(ops):
     def drift_ok(op):
         return op.kind == OP_DRIFT and not op.flags & F_EXACT and op.ints[0] == DF_MUL
 
+    def split(t):
+        if not t.flags & F_SPLITO:  # the exit keeps the original length
+            t.consts = t.consts + [t.consts[0]]
+            t.flags |= F_SPLITO
+
     out = []
     i = 0
     n = len(ops)
     while i < n:
         op = ops[i]
-        if drift_ok(op) and i + 1 < n and teapot_ok(ops[i + 1]):
-            t = ops[i + 1]
-            if not t.flags & F_SPLITO:  # the exit keeps the original length
-                t.consts = t.consts + [t.consts[0]]
-                t.flags |= F_SPLITO
-            t.consts[0] = op.consts[0] + t.consts[0]
-            t.flops += op.flops  # the algorithmic count stays the reference's
-            t.flops_fast += op.flops_fast
-            i += 1
-            continue
-        if drift_ok(op) and out and teapot_ok(out[-1]):
-            t = out[-1]
-            if not t.flags & F_SPLITO:
-                t.consts = t.consts + [t.consts[0]]
-                t.flags |= F_SPLITO
-            t.consts[-1] = t.consts[-1] + op.consts[0]
-            t.flops += op.flops
-            t.flops_fast += op.flops_fast
-            i += 1
-            continue
+        if drift_ok(op):
+            k = i + 1
+            while k < n and ops[k].kind == OP_ALIGN:
+                k += 1
+            if k < n and teapot_ok(ops[k]):  # into the entry of the next teapot
+                t = ops[k]
+                split(t)
+                t.consts[0] = op.consts[0] + t.consts[0]
+                t.flops += op.flops
+                t.flops_fast += op.flops_fast
+                i += 1
+                continue
+            k = len(out) - 1
+            while k >= 0 and out[k].kind == OP_ALIGN:
+                k -= 1
+            if k >= 0 and teapot_ok(out[k]):  # into the exit of the previous one
+                t = out[k]
+                split(t)
+                t.consts[-1] = t.consts[-1] + op.consts[0]
+                t.flops += op.flops
+                t.flops_fast += op.flops_fast
+                i += 1
+                continue
         out.append(op)
         i += 1
     return out
