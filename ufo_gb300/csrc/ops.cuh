@@ -421,7 +421,9 @@ __device__ __noinline__ PxPy kick_ool(double x, double y, double px, double py, 
 
 // ---------------------------------------------------------------- teapot
 // methods.teapot (ufo/methods.py:79-97): outer drift, N-1 x (kick, weak,
-// inner drift), kick, weak, outer drift.  Table: [outer][inner][kick][W].
+// inner drift), kick, weak, outer drift.  Table: [outer][inner][kick][W], then the exit
+// outer drift when it differs from the entry (F_SPLITO: an FMA-mode program folded a
+// neighbouring plain drift into one of them).
 //
 // The FP64 pipe of this GPU charges a predicated-off instruction like an
 // executed one, so no runtime `if` may guard FP64 arithmetic in the hot path:
@@ -435,7 +437,7 @@ __device__ __noinline__ PxPy kick_ool(double x, double y, double px, double py, 
 //   2: sextupole   a = t*x, b = t*y; px -= a*x - b*y; py += a*y + b*x,
 //                  t = (K*o)*0.5 (scaling by 0.5 commutes with rounding)
 //   3: no kick terms (bend without gradient)
-//   0: general Horner (out of line)
+//   0: general Horner (out of line; FMA mode: one complex Horner pass, kick_cplx)
 // Achromatic coefficients are multiplied by 1.0 instead of o (exact), so the
 // choice needs no branch.
 
