@@ -132,3 +132,41 @@ def test_flop_counts():
     quad = 2 * 4 + 3 * 6 + 4 * 5
     bend = 2 * 4 + 3 * 6 + 4 * 2
     assert p1.flops == 16 * (2 * quad + 2 * bend + 4 * 4)
+
+
+def test_fma_drift_merging_conserves_length_and_flops():
+    """FMA programs fold plain drifts into neighbouring teapot outer drifts:
+    the total drift length per turn, the element count and the (reference)
+    flop count are unchanged, and strict programs are not touched."""
+    import numpy as np
+    import ufo_gb300 as u
+    from ufo_gb300 import compiler as C, workloads as W
+
+    def drift_length(p):
+        tot = 0.0
+        for r in p.ops:
+            kind, fl, off = int(r[0]), int(r[1]), int(r[2])
+            c = p.table[0, off:]
+            if kind == C.OP_DRIFT:
+                assert int(r[3]) == C.DF_MUL
+                tot += c[0]
+            elif kind == C.OP_TEAPOT:
+                N, nn, ns, mn, ms = (int(v) for v in r[3:8])
+                inner = (N - 1) * (c[1] if (fl >> C.SH_FINNER) & 3 == C.DF_MUL else c[4])
+                exit_ = c[0]
+                if fl & C.F_SPLITO:
+                    k = 1 + ((1 if (fl >> C.SH_FINNER) & 3 == C.DF_MUL else 4) if N > 1 else 0)
+                    k += bin(mn).count('1') + bin(ms).count('1') + (1 if fl & C.F_WEAK else 0)
+                    exit_ = c[k]
+                tot += c[0] + exit_ + (inner if N > 1 else 0.0)
+        return tot
+
+    for ring in (W.c2_ring(u), W.c3_ring(u)):
+        strict = C.compile_line(ring, u.KICK, where=[-1])
+        fma = C.compile_line(ring, u.KICK | u.FMA, where=[-1])
+        assert len(fma.ops) < len(strict.ops)
+        assert fma.flops_fast == strict.flops_fast and fma.n_elements == strict.n_elements
+        assert abs(drift_length(fma) - drift_length(strict)) < 1e-9 * drift_length(strict)
+    assert not np.any(C.compile_line(W.c2_ring(u), u.KICK | u.FMA, where=[-1]).ops[:, 0] ==
+                      C.OP_DRIFT)
+    assert not np.any(C.compile_line(W.c2_ring(u), u.KICK, where=[-1]).ops[:, 1] & C.F_SPLITO)
