@@ -25,8 +25,8 @@ def interpret(dprog, z, o, turns=1, seed=0):
             elif kind in (D.D_TEAPOT, D.D_KICK):
                 tp = kind == D.D_TEAPOT
                 n = N if tp else 1
-                Lo, Li, W = c[0], c[1], c[2]
-                a, b = c[5:5 + M], c[5 + M:5 + 2 * M]
+                Lo, Li, W, Lx = c[0], c[1], c[2], c[5]
+                a, b = c[D.KHDR:D.KHDR + M], c[D.KHDR + M:D.KHDR + 2 * M]
                 if tp:
                     x, y = x + px * Lo, y + py * Lo
                 for sl in range(n):
@@ -37,7 +37,7 @@ def interpret(dprog, z, o, turns=1, seed=0):
                     px, py = px - oo * S.real, py + oo * S.imag
                     if tp:
                         px = px - W * x
-                        L = Li if sl < n - 1 else Lo
+                        L = Li if sl < n - 1 else Lx
                         x, y = x + px * L, y + py * L
     return np.stack([x, px, y, py], axis=1)
 

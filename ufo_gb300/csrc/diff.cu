@@ -38,7 +38,7 @@
 namespace ufo_diff {
 
 enum : int { D_NOP = 0, D_DRIFT, D_TEAPOT, D_KICK, D_ALIGN, D_EDGE };
-constexpr int KHDR = 5;   // kick constants: Lo, Li, W, g0, g1, then a[M], b[M]
+constexpr int KHDR = 6;   // kick constants: Lo, Li, W, g0, g1, Lx (exit), then a[M], b[M]
 
 struct DOp {
   int kind, flags, toff, N, M, pslot, pm, achro;
@@ -181,7 +181,7 @@ __device__ void turn_forward(St &s, const DiffArgs &a, const double *T0, double 
       case D_TEAPOT: {
         const bool tp = op.kind == D_TEAPOT;
         const int N = tp ? op.N : 1;
-        const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2);
+        const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2), Lx = __ldg(c + 5);
         if (tp) fwd_drift(s, Lo, tangent);
         for (int sl = 0; sl < N; ++sl) {
           const int k = kidx++;
@@ -197,7 +197,7 @@ __device__ void turn_forward(St &s, const DiffArgs &a, const double *T0, double 
           }
           fwd_kick(s, c + KHDR, op.M, oo, tangent);
           if (tp && W != 0.0) fwd_weak(s, W, tangent);
-          if (tp) fwd_drift(s, sl < N - 1 ? Li : Lo, tangent);
+          if (tp) fwd_drift(s, sl < N - 1 ? Li : Lx, tangent);
         }
         break;
       }
@@ -320,11 +320,11 @@ __device__ void turn_reverse(Bar &b, const DiffArgs &a, const double *T0, double
       case D_TEAPOT: {
         const bool tp = op.kind == D_TEAPOT;
         const int N = tp ? op.N : 1;
-        const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2);
+        const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2), Lx = __ldg(c + 5);
         const int pm = op.pslot >= 0 ? op.pm : -1;
         double g0 = 0.0, g1 = 0.0;
         for (int sl = N - 1; sl >= 0; --sl) {
-          if (tp) rev_drift(b, sl < N - 1 ? Li : Lo, tangent);
+          if (tp) rev_drift(b, sl < N - 1 ? Li : Lx, tangent);
           if (tp && W != 0.0) rev_weak(b, W, tangent);
           rev_kick(b, a, tt, --kidx, j, c + KHDR, op.M, oo, tangent, pm, g0, g1);
         }
@@ -498,7 +498,7 @@ __device__ __forceinline__ void kick_elem_pair(Half &h, const DiffArgs &a, const
   const double *src = c + KHDR + (even ? 0 : M);
 #pragma unroll
   for (int n = 0; n < M; ++n) cf[n] = __ldg(src + n);
-  const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2);
+  const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2), Lx = __ldg(c + 5);
   if (tp) h.u = fma(h.pu, Lo, h.u);
   for (int sl = 0; sl < N; ++sl) {
     const int k = kidx++;
@@ -530,7 +530,7 @@ __device__ __forceinline__ void kick_elem_pair(Half &h, const DiffArgs &a, const
     }
     h.pu = fma(even ? -oo : oo, r0, h.pu);
     if (tp && W != 0.0 && even) h.pu = fma(-W, h.u, h.pu);
-    if (tp) h.u = fma(h.pu, sl < N - 1 ? Li : Lo, h.u);
+    if (tp) h.u = fma(h.pu, sl < N - 1 ? Li : Lx, h.u);
   }
 }
 
@@ -571,7 +571,7 @@ __device__ void turn_forward_pair(Half &h, const DiffArgs &a, const double *T0, 
           case 8: kick_elem_pair<8>(h, a, c, tp, N, oo, even, j, write, tt, tape, kidx); continue;
           default: break;
         }
-        const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2);
+        const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2), Lx = __ldg(c + 5);
         if (tp) h.u = fma(h.pu, Lo, h.u);
         for (int sl = 0; sl < N; ++sl) {
           const int k = kidx++;
@@ -590,7 +590,7 @@ __device__ void turn_forward_pair(Half &h, const DiffArgs &a, const double *T0, 
           }
           h.pu = fma(even ? -oo : oo, s0, h.pu);
           if (tp && W != 0.0 && even) h.pu = fma(-W, h.u, h.pu);
-          if (tp) h.u = fma(h.pu, sl < N - 1 ? Li : Lo, h.u);
+          if (tp) h.u = fma(h.pu, sl < N - 1 ? Li : Lx, h.u);
         }
         break;
       }
@@ -615,10 +615,10 @@ __device__ __forceinline__ void rev_elem_pair(Half &bh, const DiffArgs &a, const
     ta[q] = t0[2 * TLANES];
     tb[q] = t0[3 * TLANES];
   }
-  const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2);
+  const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2), Lx = __ldg(c + 5);
 #pragma unroll
   for (int q = 0; q < N; ++q) {  // slice N-1-q
-    if (tp) bh.pu = fma(bh.u, q > 0 ? Li : Lo, bh.pu);
+    if (tp) bh.pu = fma(bh.u, q > 0 ? Li : Lx, bh.pu);
     if (tp && W != 0.0 && even) bh.u = fma(-W, bh.pu, bh.u);
     --kidx;
     if (write && even && kidx % CHUNK == 0 && kidx >= 2 * CHUNK)
@@ -666,7 +666,7 @@ __device__ void turn_reverse_pair(Half &bh, const DiffArgs &a, const double *T0,
       case D_TEAPOT: {
         const bool tp = op.kind == D_TEAPOT;
         const int N = tp ? op.N : 1;
-        const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2);
+        const double Lo = __ldg(c), Li = __ldg(c + 1), W = __ldg(c + 2), Lx = __ldg(c + 5);
         const int pm = op.pslot >= 0 ? op.pm : -1;
         double g0 = 0.0;
         bool done = true;
@@ -678,7 +678,7 @@ __device__ void turn_reverse_pair(Half &bh, const DiffArgs &a, const double *T0,
           default: done = false; break;
         }
         for (int sl = N - 1; !done && sl >= 0; --sl) {
-          if (tp) bh.pu = fma(bh.u, sl < N - 1 ? Li : Lo, bh.pu);
+          if (tp) bh.pu = fma(bh.u, sl < N - 1 ? Li : Lx, bh.pu);
           if (tp && W != 0.0 && even) bh.u = fma(-W, bh.pu, bh.u);
           --kidx;
           if (write && even && kidx % CHUNK == 0 && kidx >= 2 * CHUNK)

@@ -30,6 +30,7 @@ from . import compiler as C
 from .flags import FMA
 
 D_NOP, D_DRIFT, D_TEAPOT, D_KICK, D_ALIGN, D_EDGE = range(6)
+KHDR = 6  # kick constants: Lo (entry), Li, W, dK/dk/pm!, dK/dk/(pm-1)!, Lx (exit), then a, b
 
 
 def _torch():
@@ -50,9 +51,9 @@ class DiffProgram:
             np.atleast_2d(np.asarray(values, np.float64))
         if values is not None and vals.shape[1] != len(parameters):
             vals = vals.reshape(-1, len(parameters))
-        # the differentiator has its own arithmetic: compile without FMA-mode
-        # rewrites (merged drifts)
-        prog = C.compile_line(line, flags & ~FMA, parameters, [], seed_values=vals)
+        # the differentiator has its own (fused) arithmetic: it takes the FMA-mode
+        # program, whose plain drifts are folded into the magnets' outer drifts
+        prog = C.compile_line(line, flags | FMA, parameters, [], seed_values=vals)
         self.prog = prog
         flat = line.flatten() if hasattr(line, 'flatten') else list(line)
         # element index -> (parameter slot, coefficient order)
@@ -86,14 +87,15 @@ class DiffProgram:
             op = op.copy()
             op[2] = len(cols)
             if kind in (D_TEAPOT, D_KICK):
-                hdr = list(range(off, off + 5))
-                a = tab[:, off + 5:off + 5 + M]
-                b = tab[:, off + 5 + M:off + 5 + 2 * M]
+                h = KHDR
+                hdr = list(range(off, off + h))
+                a = tab[:, off + h:off + h + M]
+                b = tab[:, off + h + M:off + h + 2 * M]
                 nz = np.nonzero(np.any(a != 0, axis=0) | np.any(b != 0, axis=0))[0]
                 Mt = max(int(nz.max()) + 1 if len(nz) else 1, pm + 1 if ps >= 0 else 1)
                 op[4] = Mt
-                cols += hdr + list(range(off + 5, off + 5 + Mt)) + \
-                    list(range(off + 5 + M, off + 5 + M + Mt))
+                cols += hdr + list(range(off + h, off + h + Mt)) + \
+                    list(range(off + h + M, off + h + M + Mt))
             else:
                 n = {D_DRIFT: 1, D_ALIGN: 2, D_EDGE: 3}.get(kind, 0)
                 cols += list(range(off, off + n))
@@ -166,6 +168,9 @@ class DiffProgram:
                         ci[j] = c(q) / fac[j]
                         q += 1
                 W = c(q) if tp and fl & C.F_WEAK else 0.0
+                # exit outer drift: its own constant when a drift was merged into it
+                qx = q + (1 if tp and fl & C.F_WEAK else 0)
+                Lx = c(qx) if tp and fl & C.F_SPLITO else Lo
                 ps, pm = slot.get(elem, (-1, 0))
                 if pm >= M:  # the coefficient was truncated away (LINEAR): no effect
                     ps = -1
@@ -177,7 +182,7 @@ class DiffProgram:
                 g0 = dKdk / fac[pm] if ps >= 0 else 0.0
                 g1 = dKdk / fac[pm - 1] if ps >= 0 and pm >= 1 else 0.0
                 ops.append([D_TEAPOT if tp else D_KICK, 0, len(tab), N, M, ps, pm, achro])
-                tab += [Lo, Li, W, g0, g1] + cr + ci
+                tab += [Lo, Li, W, g0, g1, Lx] + cr + ci
                 kicks += N
             else:
                 raise NotImplementedError(f'{C.OP_NAMES[kind]} elements are not differentiated')
