@@ -506,6 +506,20 @@ def bench_c3(args):
                                          max(1, args.steps // 2))
     ms_p, launches, lost_p = runs[('sorted', False)]
     ms_plain, _, lost_plain = runs[('sorted', True)]
+    # the public API: StableAperture.run with and without its two-phase
+    # compaction (host buffers in and out, wall clock)
+    api = {}
+    for compact in (False, True):
+        sa = u.StableAperture(ring, flags=flags | u.DOUBLE_PRECISION, turns=T, particles=n,
+                              parameters=['x', 'px', 'y', 'py', 'dp'], context=ctx)
+        sa.parameters[:] = grid[:, [0, 1, 2, 3, 5]]
+        sa.run(compact=compact)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sa.run(compact=compact)
+        api[compact] = (time.perf_counter() - t0, sa.lost.astype(np.int64).copy(),
+                        getattr(sa, 'second_phase_warps_per_sm', None),
+                        getattr(sa, 'survivors_after_first_phase', None))
     clk = clocks.stop()
     peak = ctypes_peak(ctx)
     # a particle lost at the end of turn t tracked t + 1 turns
@@ -542,9 +556,25 @@ def bench_c3(args):
                 'persistent': pet / (runs[('amplitude', False)][0] / 1e3),
                 'plain': pet / (runs[('amplitude', True)][0] / 1e3),
                 'note': 'the same grid, largest amplitude (then |dp|) first'},
+            'stable_aperture_api': {
+                'one_phase': {'value': pet / api[False][0], 's': api[False][0]},
+                'two_phase_compaction': {
+                    'value': pet / api[True][0], 's': api[True][0],
+                    'survivors_after_turns_div_8': api[True][3],
+                    'second_phase_warps_per_sm': api[True][2]},
+                'note': 'StableAperture.run end to end (host buffers); the two-phase run '
+                        'tracks turns/8 on the full grid, then only the survivors on a grid '
+                        'sized to them'},
             'identical_loss_turns': bool(all(np.array_equal(lost_p, r[2])
-                                             for r in runs.values())),
-            'gpu_launches': launches}
+                                             for r in runs.values()) and
+                                         np.array_equal(api[False][1], lost_p) and
+                                         np.array_equal(api[True][1], lost_p)),
+            'gpu_launches': launches,
+            'e2e': {'value': pet / api[True][0], 'unit': 'particle*element*turns/s',
+                    'h2d_bytes_per_step': n * 6 * 8,
+                    'd2h_bytes_per_step': n * (6 * 8 + 4),
+                    'api': 'ufo_gb300.StableAperture(...).run() (two-phase compaction, host '
+                           'buffers)'}}
     if clk:
         line['clocks'] = clk
     print(json.dumps(line), flush=True)

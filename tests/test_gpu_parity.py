@@ -191,6 +191,27 @@ def test_c3_full_grid_subset_loss_turns_vs_oracle():
     assert np.array_equal(lp, lq)
 
 
+def test_stable_aperture_two_phase_is_identical():
+    """StableAperture's compaction (first turns/8 on the full grid, the
+    survivors on a grid sized to them) gives the loss turns and coordinates of
+    one run, bit for bit, in strict and FMA modes."""
+    import ufo_gb300 as u
+    from ufo_gb300 import workloads as W
+    ring = W.c3_ring(u)
+    grid = W.c3_grid(48, 48)
+    for flags in (u.KICK | u.DOUBLE_PRECISION, u.KICK | u.FMA | u.DOUBLE_PRECISION):
+        out = []
+        for compact in (False, True):
+            sa = u.StableAperture(ring, flags=flags, turns=600, particles=len(grid),
+                                  parameters=['x', 'px', 'y', 'py', 'dp'])
+            sa.parameters[:] = grid[:, [0, 1, 2, 3, 5]]
+            sa.run(compact=compact)
+            out.append((sa.lost.copy(), sa.final.copy()))
+        assert np.array_equal(out[0][0], out[1][0])
+        assert np.array_equal(out[0][1], out[1][1], equal_nan=True)
+        assert 0 < np.sum(out[0][0] < 600) < len(grid)
+
+
 def test_seed_batch_equals_individual_launches():
     """One launch over many error seeds == one launch per seed, bit for bit."""
     import ufo_gb300 as u

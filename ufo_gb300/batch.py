@@ -240,7 +240,7 @@ def autotune(batch, warps=(8, 12, 16), orders=('lpt', 'seed'), scale=16, use_cac
                 for order in orders:
                     batch.upload(order)
                     for w in warps:
-                        capi.check(capi.load().ufo_ctx_set_tuning(batch.ctx.handle, int(w)))
+                        batch.ctx.set_tuning(w)
                         batch.launch(stream=stream.cuda_stream, graph=False)  # warm
                         stream.synchronize()
                         e0 = torch.cuda.Event(enable_timing=True)
@@ -265,6 +265,6 @@ def autotune(batch, warps=(8, 12, 16), orders=('lpt', 'seed'), scale=16, use_cac
                     json.dump(cache, f, indent=1)
             except OSError:
                 pass
-    capi.check(capi.load().ufo_ctx_set_tuning(batch.ctx.handle, int(best['warps_per_sm'])))
+    batch.ctx.set_tuning(best['warps_per_sm'])
     batch.order = best['order']
     return best

@@ -120,6 +120,13 @@ class Context:
         self.handle = h
         self.device = device
 
+    warps_per_sm = 16  # resident warps per SM of the persistent grid (library default)
+
+    def set_tuning(self, warps_per_sm):
+        """ufo_ctx_set_tuning, remembered so that callers can restore it."""
+        check(load().ufo_ctx_set_tuning(self.handle, int(warps_per_sm)))
+        self.warps_per_sm = int(warps_per_sm)
+
     def launches(self):
         n = ctypes.c_int64()
         check(load().ufo_launch_count(self.handle, ctypes.byref(n)))

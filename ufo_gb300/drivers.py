@@ -194,6 +194,11 @@ class Track:
         self.final = final.astype(self.final.dtype, copy=False)
 
 
+def _sm_count(device):
+    import torch
+    return torch.cuda.get_device_properties(device).multi_processor_count
+
+
 class StableAperture:
     """Turns survived per particle (ufo/sa.py:18-145): lost at the end of the
     first turn with |x| > 1 or |y| > 1 or isnan(x); ``lost`` holds that turn,
@@ -219,13 +224,56 @@ class StableAperture:
     def program(self):
         return self._c.prog
 
-    def run(self, threads=1):
+    def _uses_turn(self):
+        import re
+        return any(type(e).__name__ == 'Aperture' and re.search(r'\bturn\b', str(e.window))
+                   for e in self._line.flatten())
+
+    def run(self, threads=1, compact=None):
+        """``compact`` (default: for 512+ turns and 16,384+ particles): track
+        the first turns/8 with the full persistent grid, then continue only the
+        survivors with a grid sized to them (resident warps per SM about
+        survivors / (0.9 x 32 x SMs)), so that the long-lived particles fill
+        whole warps; loss turns and coordinates are those of one run.  Not
+        used when an aperture window reads ``turn``."""
         pool = np.asarray(self.parameters, dtype=np.float64)
         seed_values, seed = self._c.seeds(pool)
         dprog = self._c.device(self.ctx, seed_values)
         coords = _coords_from_pool(pool, self._names, self.flags, self.dp)
-        _, lost, final = capi.track(self.ctx, dprog, coords, self.turns, capi.UFO_MODE_SA,
-                                    _track_flags(self.flags), seed=seed, slots=0)
+        T, n = int(self.turns), coords.shape[0]
+        if compact is None:
+            compact = T >= 512 and n >= 16384
+        if compact and self._uses_turn():
+            compact = False
+        flags = _track_flags(self.flags)
+        if not compact:
+            _, lost, final = capi.track(self.ctx, dprog, coords, T, capi.UFO_MODE_SA, flags,
+                                        seed=seed, slots=0)
+            self.lost = lost
+            self.final = final
+            return
+        T1 = max(1, T // 8)
+        _, lost, final = capi.track(self.ctx, dprog, coords, T1, capi.UFO_MODE_SA, flags,
+                                    seed=seed, slots=0)
+        alive = np.nonzero(lost >= T1)[0]
+        self.survivors_after_first_phase = len(alive)
+        if len(alive) and T > T1:
+            sms = _sm_count(self.ctx.device)
+            warps = int(min(16, max(2, round(len(alive) / (0.9 * 32 * sms)))))
+            self.second_phase_warps_per_sm = warps
+            before = self.ctx.warps_per_sm
+            self.ctx.set_tuning(warps)
+            try:
+                _, lost2, final2 = capi.track(
+                    self.ctx, dprog, np.ascontiguousarray(final[alive]), T - T1,
+                    capi.UFO_MODE_SA, flags,
+                    seed=None if seed is None else np.ascontiguousarray(seed[alive]), slots=0)
+            finally:
+                self.ctx.set_tuning(before)
+            lost = lost.copy()
+            lost[alive] = T1 + lost2
+            final = final.copy()
+            final[alive] = final2
         self.lost = lost
         self.final = final
 
