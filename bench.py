@@ -211,10 +211,10 @@ def bench_ours(args):
     from ufo_gb300 import capi, compiler as C, workloads as W
     from ufo_gb300.ranks import beam_seed, max_over_ranks
     world, rank, local = dist()
+    torch.cuda.set_device(local)  # before the process group: NCCL binds the current device
     if world > 1:
         import torch.distributed as tdist
         tdist.init_process_group('nccl')
-    torch.cuda.set_device(local)
     dev = torch.device('cuda', local)
     ctx = u.context(local)
     ring = W.c2_ring(u)
