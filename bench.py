@@ -66,6 +66,8 @@ def parse():
                     help='C5: error seeds in the GPU-filling adjoint batch')
     ap.add_argument('--c5-fd-params', type=int, default=8,
                     help='C5: parameters in the sampled multi-turn FD')
+    ap.add_argument('--fp64-probe', action='store_true',
+                    help='print the FP64-pipe probe table (latency, occupancy, active lanes)')
     ap.add_argument('--c5-skip-multiturn', action='store_true',
                     help='C5: optics gradients only (for profiling captures)')
     return ap.parse_args()
@@ -828,8 +830,29 @@ def ctypes_peak(ctx):
     return g.value
 
 
+def fp64_probe():
+    """The FP64 pipe under controlled conditions: resident warps per SM,
+    independent DFMA chains per thread, active lanes per warp."""
+    import ctypes
+    import ufo_gb300 as u
+    from ufo_gb300 import capi
+    ctx = u.context(0)
+    lib = capi.load()
+    rows = []
+    for w, ch, lanes in ((4, 1, 32), (4, 8, 32), (16, 1, 32), (16, 8, 32), (32, 8, 32),
+                         (16, 8, 16), (16, 8, 8), (16, 8, 1)):
+        g = ctypes.c_double()
+        capi.check(lib.ufo_fp64_probe(ctx.handle, w, ch, lanes, ctypes.byref(g)))
+        rows.append({'warps_per_sm': w, 'chains_per_thread': ch, 'active_lanes': lanes,
+                     'useful_gflops': g.value})
+    print(json.dumps({'fp64_probe': rows, 'fp64_peak_gflops': ctypes_peak(ctx)}), flush=True)
+
+
 def main():
     args = parse()
+    if args.fp64_probe:
+        fp64_probe()
+        return
     if args.impl == 'reference':
         bench_reference(args)
     elif args.workload == 'c3':

@@ -191,6 +191,12 @@ int ufo_launch_count(ufo_ctx *ctx, int64_t *count);
  * (the roofline denominator of the benchmark); no reference counterpart. */
 int ufo_fp64_peak(ufo_ctx *ctx, double *gflops);
 
+/* FP64-pipe probe (no reference counterpart): one-warp blocks, `warps_per_sm`
+ * per SM, `chains` (1, 2, 4 or 8) independent DFMA chains per thread, only the
+ * first `lanes` lanes of each warp active; *gflops counts the active lanes'
+ * flops (2 per DFMA).  Shows what latency, occupancy and inactive lanes cost. */
+int ufo_fp64_probe(ufo_ctx *ctx, int warps_per_sm, int chains, int lanes, double *gflops);
+
 #ifdef __cplusplus
 }
 #endif

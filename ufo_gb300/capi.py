@@ -51,6 +51,7 @@ SIGNATURES = {
                          ctypes.c_int, P, P, P, P],
     'ufo_launch_count': [P, P],
     'ufo_fp64_peak': [P, P],
+    'ufo_fp64_probe': [P, ctypes.c_int, ctypes.c_int, ctypes.c_int, P],
     'ufo_ctx_set_tuning': [P, ctypes.c_int],
     'ufo_closed_orbit': [P, P, P, P, I64, ctypes.c_int, P],
     'ufo_graph_create': [P, P, P, P, P, I64, ctypes.c_int, ctypes.c_int, ctypes.c_int, I64,

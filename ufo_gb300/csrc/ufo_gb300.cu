@@ -370,6 +370,27 @@ __global__ void __launch_bounds__(256) dfma_peak_kernel(double *out, int iters, 
   out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// FP64 pipe probe: CH independent DFMA chains per thread; only the first
+// `lanes` lanes of each warp run the chains (the rest skip the loop), so the
+// useful rate shows what inactive lanes cost
+template <int CH>
+__global__ void __launch_bounds__(32) dfma_probe_kernel(double *out, int iters, int lanes,
+                                                        double b, double c) {
+  double a[CH];
+#pragma unroll
+  for (int k = 0; k < CH; ++k) a[k] = threadIdx.x * 1e-3 + k;
+  if (static_cast<int>(threadIdx.x & 31) < lanes) {
+    for (int i = 0; i < iters; ++i) {
+#pragma unroll
+      for (int k = 0; k < CH; ++k) a[k] = fma_(a[k], b, c);
+    }
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < CH; ++k) s = add(s, a[k]);
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace ufo
 
 // ======================================================================= C ABI
@@ -713,6 +734,46 @@ int ufo_fp64_peak(ufo_ctx *ctx, double *gflops) {
   cudaFree(buf);
   if (err != cudaSuccess) return cuda_fail(err, "fp64 peak probe");
   *gflops = 2.0 * blocks * threads * static_cast<double>(iters) * 8 / (best * 1e6);
+  return UFO_OK;
+}
+
+int ufo_fp64_probe(ufo_ctx *ctx, int warps_per_sm, int chains, int lanes, double *gflops) {
+  if (!ctx || !gflops) return fail(UFO_E_ARG, "null argument");
+  if (warps_per_sm < 1 || warps_per_sm > 32) return fail(UFO_E_ARG, "warps_per_sm in [1, 32]");
+  if (lanes < 1 || lanes > 32) return fail(UFO_E_ARG, "lanes in [1, 32]");
+  if (chains != 1 && chains != 2 && chains != 4 && chains != 8)
+    return fail(UFO_E_ARG, "chains in {1, 2, 4, 8}");
+  UFO_CUDA(cudaSetDevice(ctx->device));
+  const int blocks = ctx->sm_count * warps_per_sm, iters = 32768 / chains;
+  double *buf = nullptr;
+  if (cudaMalloc(&buf, sizeof(double) * blocks * 32) != cudaSuccess)
+    return fail(UFO_E_NOMEM, "cudaMalloc(probe buffer)");
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 1e30f;
+  cudaError_t err = cudaSuccess;
+  for (int rep = 0; rep < 4 && err == cudaSuccess; ++rep) {
+    cudaEventRecord(e0, ctx->stream);
+    switch (chains) {
+      case 1: ufo::dfma_probe_kernel<1><<<blocks, 32, 0, ctx->stream>>>(buf, iters, lanes, 0.999999, 1e-7); break;
+      case 2: ufo::dfma_probe_kernel<2><<<blocks, 32, 0, ctx->stream>>>(buf, iters, lanes, 0.999999, 1e-7); break;
+      case 4: ufo::dfma_probe_kernel<4><<<blocks, 32, 0, ctx->stream>>>(buf, iters, lanes, 0.999999, 1e-7); break;
+      default: ufo::dfma_probe_kernel<8><<<blocks, 32, 0, ctx->stream>>>(buf, iters, lanes, 0.999999, 1e-7); break;
+    }
+    cudaEventRecord(e1, ctx->stream);
+    err = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (rep > 0 && ms < best) best = ms;
+  }
+  if (err == cudaSuccess) err = cudaGetLastError();
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(buf);
+  if (err != cudaSuccess) return cuda_fail(err, "fp64 probe");
+  // useful flops: active lanes only
+  *gflops = 2.0 * blocks * lanes * static_cast<double>(iters) * chains / (best * 1e6);
   return UFO_OK;
 }
 
