@@ -209,7 +209,7 @@ def _key(batch):
     return f'{torch.cuda.get_device_name(batch.ctx.device)}|{batch.n}|{h.hexdigest()[:16]}'
 
 
-def autotune(batch, warps=(8, 12, 16), orders=('lpt', 'seed'), scale=16, use_cache=True):
+def autotune(batch, warps=(6, 8, 10, 12, 16), orders=('lpt', 'seed'), scale=16, use_cache=True):
     """Choose resident warps per SM and the particle order for ``batch``.
 
     Candidates are timed with CUDA events on a copy of the workload whose turn
