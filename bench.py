@@ -659,6 +659,39 @@ def _c5_multiturn(args, u, W, torch, ctx, stream, model, ring, params, vals, rng
     fdp2 = (ampp2[0::2] - ampp2[1::2]) / (2 * hm[:, None])
     rel2 = np.abs(g[idx] - fdp2[:, obj].sum(axis=1)) / np.abs(fdp2[:, obj]).sum(axis=1)
     launches += efd.launches
+    del efd, zf
+    # a 4-point stencil (f(k-2h) - 8 f(k-h) + 8 f(k+h) - f(k+2h)) / 12h of the
+    # same map at two steps: its truncation error falls as h^4 and its rounding
+    # noise as 1/h, so at h = 1e-6..4e-6 (relative) it resolves the derivative
+    # far below a central difference at h = 1e-7; the two steps' disagreement
+    # is the stencil's own error estimate (accuracy only, not timed)
+    steps4 = (1e-6, 4e-6)
+    offs = np.array([2.0, 1.0, -1.0, -2.0])
+    rows4, h4s = [], []
+    for hr in steps4:
+        h4 = hr * np.abs(vals[idx])
+        h4s.append(h4)
+        r = np.repeat(vals[None], 4 * m, 0)
+        for q, c in enumerate(offs):
+            r[q::4][np.arange(m), idx] += c * h4
+        rows4.append(r)
+    rows4 = np.concatenate(rows4)
+    e4 = D.DiffEngine(D.DiffProgram(ring, u.KICK, params, rows4))
+    z4, _ = e4.forward(np.tile(coords[:, :4], (len(rows4), 1)), np.tile(o, len(rows4)), T,
+                       seed=np.repeat(np.arange(len(rows4), dtype=np.int32), Np))
+    launches += e4.launches
+    amp4 = (z4[:, 0] ** 2 + z4[:, 2] ** 2).reshape(len(steps4), m, 4, Np)
+    del e4, z4
+    st4 = {}
+    fd4 = []
+    for s, hr in enumerate(steps4):
+        a4 = amp4[s]
+        d = (-a4[:, 0] + 8 * a4[:, 1] - 8 * a4[:, 2] + a4[:, 3]) / (12 * h4s[s][:, None])
+        fd4.append(d)
+        st4[f'{hr:g}'] = float(np.max(np.abs(g[idx] - d[:, obj].sum(axis=1)) /
+                                      np.abs(d[:, obj]).sum(axis=1)))
+    stencil_self = float(np.max(np.abs(fd4[0][:, obj].sum(axis=1) - fd4[1][:, obj].sum(axis=1)) /
+                                np.abs(fd4[0][:, obj]).sum(axis=1)))
     # the per-particle cotangents do not depend on the mask: the same
     # comparison over stricter regularity thresholds
     by_thr = {}
@@ -684,10 +717,14 @@ def _c5_multiturn(args, u, W, torch, ctx, stream, model, ring, params, vals, rng
         'rel_err_per_param': rel.tolist(),
         'rel_err_note': '|sum(adjoint - FD)| / sum|per-particle FD| over the regular '
                         'particles; FD through the tracking kernel (FMA mode); '
-                        '_fd_same_map: through the differentiator\'s forward map',
+                        '_fd_same_map: through the differentiator\'s forward map; '
+                        '4pt_stencil: (f(k-2h) - 8f(k-h) + 8f(k+h) - f(k+2h)) / 12h of '
+                        'the same map at the relative steps named',
         'sampled_params': [params[i] for i in idx],
         'rel_err_per_param_fd_same_map': rel2.tolist(),
         'same_map_by_growth_threshold': by_thr,
+        'max_rel_err_vs_4pt_stencil_same_map': st4,
+        'stencil_steps_disagreement': stencil_self,
         'per_particle_median_rel_err': float(np.median(pp))}
     return out, launches
 
