@@ -18,7 +18,7 @@ UFO_TRACK_FMA, UFO_TRACK_FIVED, UFO_TRACK_PLAIN = 1, 2, 4
 
 _lib = None
 _lock = threading.Lock()
-_exiting = False  # set at interpreter exit: destructors then leave teardown to the driver
+_exiting = False  # set at interpreter exit: destructors then leave teardown to the CUDA driver
 
 
 def _mark_exit():

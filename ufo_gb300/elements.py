@@ -76,7 +76,7 @@ class Element:
         return {'kind': self.kind}
 
     def survey(self, x0=None, alpha0=0.):
-        raise NotImplementedError('survey() is outside the tracking path of this build')
+        raise NotImplementedError('survey() (element positions) is not part of the tracking library')
 
 
 class Marker(Element):
