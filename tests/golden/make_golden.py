@@ -166,7 +166,8 @@ def main(ref):
             np.stack([xx.ravel(), yy.ravel()], 1), ['x', 'y'])
 
     # --- optics: tunes, chromaticity by finite differences, thick vs kick, align
-    def optics_case(name, line, flags, where, periodic=True, params=(), pval=None, attrs=None):
+    def optics_case(name, line, flags, where, periodic=True, params=(), pval=None, attrs=None,
+                    consumers=False):
         o = ufo.Optics(line, where=list(where), periodic=periodic, parameters=list(params),
                        flags=flags)
         if pval is not None:
@@ -180,6 +181,14 @@ def main(ref):
         for k in ('qx', 'qy'):
             if hasattr(o, k):
                 outs[k] = np.float64(getattr(o, k))
+        if consumers:
+            # the reference's host consumers of the optics output
+            # (ufo/radiation.py, ufo/chroma.py)
+            rad = ufo.emittance(o)
+            for k in ('I1', 'I2', 'I4', 'I5', 'Jx', 'Jt', 'U0', 'Ex'):
+                outs[f'rad_{k}'] = np.float64(getattr(rad, k))
+            (dqx0, dqy0), (dqx, dqy) = ufo.chromaticity(o)
+            outs['chroma'] = np.array([dqx0, dqy0, dqx, dqy], dtype=np.float64)
         add(name, 'optics', line, flags, dict(where=list(where), periodic=periodic,
                                               parameters=list(params),
                                               pval=None if pval is None else float(pval),
@@ -201,6 +210,14 @@ def main(ref):
                 attrs=dict(ax0=float(o64.ax[-1]), ay0=float(o64.ay[-1]), bx0=float(o64.bx[-1]),
                            by0=float(o64.by[-1]), dx0=float(o64.dx[-1]),
                            dpx0=float(o64.dpx[-1])))
+    # radiation integrals and analytic chromaticity, as the reference's tests
+    # call them (tests/radiation.py:17-21, tests/chroma.py:12-17)
+    bends = lat('alba.mad').find(lambda e: hasattr(e, 'angle'))
+    mags = lat('alba.mad').find(lambda e: hasattr(e, 'k1') or hasattr(e, 'k2'))
+    for tag, fl in (('fp32', ufo.LINEAR | ufo.ACHROMATIC),
+                    ('fp64', ufo.LINEAR | ufo.ACHROMATIC | ufo.DOUBLE_PRECISION)):
+        optics_case(f'alba_radiation_{tag}', lat('alba.mad'), fl, bends, consumers=True)
+        optics_case(f'alba_chroma_{tag}', lat('alba.mad'), fl, mags, consumers=True)
     ufo.DEFAULT_QUADRUPOLE_SLICES, ufo.DEFAULT_BEND_SLICES = 16, 48
     tk = lat('alba.mad')
     ufo.DEFAULT_QUADRUPOLE_SLICES, ufo.DEFAULT_BEND_SLICES = 8, 8
@@ -242,6 +259,11 @@ def main(ref):
     madx['tracking_fodo_x'] = [float(v) for v in arr.replace('\n', ' ').split(',')]
     madx['alba_qx'], madx['alba_qy'] = floats('optics.py', r'q[xy] = ([-\d.]+)')
     madx['alba_dqx'], madx['alba_dqy'] = floats('optics3.py', r'dq[xy]_mad = ([-\d.]+)')
+    rad = dict(re.findall(r'^\s*(I[1245]|alpha_c)\s*=\s*([-\d.e]+)',
+                          open(os.path.join(ref, 'tests', 'radiation.py')).read(), re.M))
+    for k, v in rad.items():
+        madx[f'alba_{k}'] = float(v)
+    madx['alba_dqx_sext'], madx['alba_dqy_sext'] = floats('chroma.py', r'dq[xy] = ([-\d.]+)')
 
     with open(os.path.join(HERE, 'cases.json'), 'w') as f:
         json.dump({'cases': cases, 'lattices': lattices, 'madx': madx,

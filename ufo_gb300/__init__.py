@@ -2,7 +2,8 @@
 
 The names below mirror the reference's package exports (ufo/__init__.py:3-23)
 for the tracking path: lattices and elements, ``Track``, ``StableAperture``,
-``ClosedOrbit``, ``Optics``, ``chromaticity``, the flags and the
+``ClosedOrbit``, ``Optics``, ``chromaticity``, ``emittance`` /
+``RadiationIntegrals``, ``Beam``, the physical constants, the flags and the
 ``DEFAULT_*_SLICES`` knobs.  The OpenCL context plumbing
 (``list_devices``/``context``) becomes CUDA device selection.
 """
@@ -16,7 +17,9 @@ from .flags import (LINEAR, FIVED, EXACT, KICK, RADIATION, DOUBLE_PRECISION,  # 
                     ACHROMATIC, YOSHIDA, FMA)
 from .elements import (Element, Marker, Drift, Multipole, Quadrupole, Sbend, Rbend,  # noqa: E402
                        Sextupole, Octupole, Wire, Aperture)
-from .lattice import Lattice, Line  # noqa: E402
+from .lattice import Lattice, Line, Beam  # noqa: E402
+from .constants import *  # noqa: E402,F401,F403
+from .radiation import emittance, RadiationIntegrals  # noqa: E402
 
 
 def __getattr__(name):

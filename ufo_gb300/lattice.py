@@ -79,3 +79,23 @@ class Line(list):
         prog = compiler.compile_line(self, flags=flags, parameters=parameters or [],
                                      where=fracture or [])
         return prog.segments
+
+
+class Beam:
+    """Beam description (ufo/lattice.py:152-164): energy in eV, particle mass
+    in eV, bunch charge, current, emittances, bunch length and energy spread.
+    ``gamma`` is (1 + energy) / mass as the reference computes it (the 1 eV
+    offset is below 1e-9 relative at GeV energies)."""
+
+    def __init__(self, energy=3e9, particle_mass=None, bunch_charge=1e-9, beam_current=0.25,
+                 ex=1e-9, ey=1e-9, bunch_length=6e-3, energy_spread=1e-3):
+        from .constants import electron_mass
+        self.energy = energy
+        self.particle_mass = electron_mass if particle_mass is None else particle_mass
+        self.gamma = (1. + energy) / self.particle_mass
+        self.bunch_charge = bunch_charge
+        self.beam_current = beam_current
+        self.ex = ex
+        self.ey = ey
+        self.bunch_length = bunch_length
+        self.energy_spread = energy_spread
