@@ -9,7 +9,11 @@ per-seed element records.  Attribute resolution follows the reference's
 element ``method()``s (``value or self.value``, ufo/elements.py) and
 parameter binding follows ufo/lattice.py:107-110; transcendentals that the
 reference's C compiler would fold (literal arguments) are precomputed here,
-correctly rounded, exactly as GCC folds them.
+correctly rounded, exactly as GCC folds them.  Elements whose class has its
+own ``method()`` (time-dependent kickers) are called as the reference's
+Line.method calls them; the C text they return is parsed with ufo_gb300's
+expression parser (cexpr) and evaluated here in C with the C library's math,
+as the reference's compiled kernel evaluates it.
 """
 import ctypes
 import math
@@ -126,6 +130,12 @@ class Prepared:
                 r = elems[s * n + idx]
                 prm = binds[idx]
                 lit = {}
+                if _user_method(e):
+                    self._dynamic_multipole(r, e, prm, flags, per[idx], seed_values[s], ap)
+                    r['nfrac'] = len(per[idx])
+                    r['frac_off'] = frac_off[idx]
+                    r['pre_dump'] = int(pre[idx])
+                    continue
 
                 def get(name, default=0.0):
                     if name in prm:
@@ -241,10 +251,60 @@ class Prepared:
                             fl += v
                 fold += fl
         self.elems = elems
+        self.ap_list = ap
         self.mp = np.array(mp + [0.0], dtype=np.float64)
         self.fr = np.array(fr + [0.0], dtype=np.float64)
         self.fold = np.array(fold + [0.0], dtype=np.float64)
         self.ap = np.array(ap + [0.0], dtype=np.float64)
+
+
+    @staticmethod
+    def _dynamic_multipole(r, e, prm, flags, fracture, row, ap):
+        """A multipole subclass with its own method(): called as
+        ufo/lattice.py:107-113 calls it (bound parameters as the text
+        ``parameters[i]``); the values it hands its base class (C text or
+        numbers) become one program per coefficient (the base class
+        ufo/elements.py:152-167: ``knl`` / ``kN`` overrides, ``dx or
+        self.dx``)."""
+        from ufo_gb300 import cexpr, elements
+        if e.kind != 'multipole':
+            raise NotImplementedError('user pass methods of thin multipoles only')
+        out = e.method(flags=flags, fracture=list(fracture),
+                       **{name: f'parameters[{col}]' for name, col in prm.items()})
+        vals = [p for p in out if isinstance(p, elements.PassMethod)][0].values
+        knl = list(vals['knl']) if vals.get('knl') is not None else list(e.knl)
+        ksl = list(vals['ksl']) if vals.get('ksl') is not None else list(e.ksl)
+        for p, v in vals.items():
+            if p[:1] == 'k' and p[1:].isdigit():
+                knl[int(p[1:])] = v
+            if p[:1] == 'k' and p[-1:] == 's' and p[1:-1].isdigit():
+                ksl[int(p[1:-1])] = v
+
+        def program(v):
+            if isinstance(v, str):
+                code, _, _ = cexpr.compile_expr(v, allow_params=True)
+                return [(cexpr.PUSH, float(row[int(x)])) if op == cexpr.PARAM else (op, x)
+                        for op, x in code]
+            return [(cexpr.PUSH, float(v))]
+
+        def number(name):
+            v = vals.get(name) or getattr(e, name)
+            return cexpr.evaluate(program(v)) if isinstance(v, str) else float(v)
+        r['type'] = 10
+        r['dx'], r['dy'] = number('dx'), number('dy')
+        r['nknl'], r['nksl'] = len(knl), len(ksl)
+        r['ap_off'] = len(ap)
+        for v in knl + ksl:
+            code = program(v)
+            ap.append(float(len(code)))
+            for op, x in code:
+                ap += [float(op), float(x)]
+        r['ap_len'] = len(ap) - r['ap_off']
+
+
+def _user_method(e):
+    from ufo_gb300 import elements
+    return type(e).method is not elements.Element.method
 
 
 def _ptr(a):

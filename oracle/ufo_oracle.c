@@ -40,7 +40,7 @@
 #define F_ACHRO 64
 
 enum { T_MARKER = 0, T_DRIFT, T_MULTIPOLE, T_QUAD, T_SBEND, T_RBEND, T_SEXT, T_OCT, T_WIRE,
-       T_APERTURE };
+       T_APERTURE, T_DYNMULT };
 
 /* one flat element of one seed; lists live in `mp`, fractures in `frac`,
  * folded transcendentals in `fold`, aperture programs in `ap` */
@@ -222,8 +222,8 @@ static void wire_(state *s, double wx, double wy, double wk) {
     s->py += B * sin(alpha);
 }
 
-/* stack program of the loss test ``{window} == 0`` (see ufo_gb300/aperture.py) */
-static int aperture_lost_(const state *s, const double *prog, int n) {
+/* value of a C-expression stack program (opcodes of ufo_gb300/cexpr.py) */
+static double eval_(const state *s, const double *prog, int n) {
     double st[32];
     int sp = 0;
     const double vars[8] = {s->x, s->px, s->y, s->py, s->z, s->dp, s->oodppo, (double)s->turn};
@@ -238,6 +238,13 @@ static int aperture_lost_(const state *s, const double *prog, int n) {
         case 4: st[sp - 1] = st[sp - 1] == 0 ? 1. : 0.; break;
         case 19: st[sp - 1] = fabs(st[sp - 1]); break;
         case 20: st[sp - 1] = sqrt(st[sp - 1]); break;
+        case 22: st[sp - 1] = sin(st[sp - 1]); break;
+        case 23: st[sp - 1] = cos(st[sp - 1]); break;
+        case 24: st[sp - 1] = tan(st[sp - 1]); break;
+        case 25: st[sp - 1] = exp(st[sp - 1]); break;
+        case 26: st[sp - 1] = log(st[sp - 1]); break;
+        case 27: st[sp - 1] = (double)(float)st[sp - 1]; break;
+        case 28: st[sp - 1] = trunc(st[sp - 1]); break;
         case 21: b = st[--sp]; a = st[--sp]; c = st[--sp]; st[sp++] = c != 0 ? a : b; break;
         default:
             b = st[--sp];
@@ -261,7 +268,12 @@ static int aperture_lost_(const state *s, const double *prog, int n) {
             st[sp++] = c;
         }
     }
-    return st[sp - 1] != 0;
+    return st[sp - 1];
+}
+
+/* the loss test ``{window} == 0`` (see ufo_gb300/aperture.py) */
+static int aperture_lost_(const state *s, const double *prog, int n) {
+    return eval_(s, prog, n) != 0;
 }
 
 typedef struct {
@@ -313,6 +325,21 @@ static void one_turn_(state *s, int flags, const oelem *el, int n, const double 
         case T_APERTURE:
             if (aperture_lost_(s, ap + q->ap_off, q->ap_len)) s->x = NAN;
             break;
+        case T_DYNMULT: {
+            /* a multipole whose coefficients are C text of a user pass method:
+             * each evaluated where the reference's kick statement reads it */
+            align_(s, q->dx, q->dy);
+            const double *pq = ap + q->ap_off;
+            for (int j = 0; j < q->nknl + q->nksl && j < 256; ++j) {
+                const int len = (int)pq[0];
+                const double v = eval_(s, pq + 1, len);
+                if (j < q->nknl) knl[j] = v; else ksl[j - q->nknl] = v;
+                pq += 1 + 2 * len;
+            }
+            kick_(s, flags, knl, q->nknl, ksl, q->nksl);
+            align_(s, -(q->dx), -(q->dy));
+            break;
+        }
         default:
             for (int i = 0; i < np; ++i) {
                 const double f1 = i < q->nfrac ? fr[q->frac_off + i] : 1.;

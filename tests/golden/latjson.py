@@ -33,8 +33,12 @@ def _val(v):
 def dump(line):
     out = []
     for e in line.flatten():
-        cls = type(e).__name__
+        # a user subclass (e.g. a kicker overriding method()) is stored as its
+        # library base class; its own behaviour is described by the case
+        cls = next(c.__name__ for c in type(e).__mro__ if c.__name__ in ATTRS)
         d = {'class': cls, 'label': e.label}
+        if cls != type(e).__name__:
+            d['subclass'] = type(e).__name__
         for a in ATTRS[cls]:
             d[a] = _val(e.__dict__[a])
         out.append(d)
@@ -49,6 +53,7 @@ def load(items, m=None):
         d = dict(d)
         cls = getattr(m, d.pop('class'))
         label = d.pop('label')
+        d.pop('subclass', None)
         els.append(cls(label, **d))
     return m.Line('RING', els)
 

@@ -229,6 +229,48 @@ def main(ref):
     optics_case('align_equiv', al.EQUIVALENT, ufo.LINEAR | ufo.ACHROMATIC | ufo.DOUBLE_PRECISION,
                 [-1])
 
+    # --- time-dependent user elements: subclasses overriding method() with C
+    # text of `turn` (the two kickers of HOWTO.md:84-200, on the ALBA ring)
+    class NLKGate(ufo.Multipole):
+        def method(self, k1=None, **kwargs):
+            k1 = k1 or self.knl[1]
+            return super().method(k1=f'((turn == 20) ? {k1} : 0.)', **kwargs)
+
+    class NLKPulse(ufo.Multipole):
+        def __init__(self, label, t0=0., tau=0., **kwargs):
+            super().__init__(label, **kwargs)
+            self.tau = tau
+            self.t0 = t0
+            self.parameters += ['tau', 't0']
+
+        def method(self, k1=None, t0=None, tau=None, **kwargs):
+            k1, t0, tau = k1 or self.knl[1], t0 or self.t0, tau or self.tau
+            k = (f'((turn >= {t0}) && (turn < {t0} + {tau}) )? '
+                 f'{k1} * sin(3.1415 * ((float)turn - {t0}) / {tau}): 0.')
+            return super().method(k1=f'({k})', **kwargs)
+
+    rng = np.random.default_rng(7)
+    betax, ex0 = 11.26, 4.3e-9
+    for name, kicker, turns, n, params, extra in (
+            ('nlk_gate', NLKGate('NLK', knl=[0., 5e-2]), 40, 32, ['x', 'px'], {}),
+            ('nlk_pulse', NLKPulse('NLK', knl=[0., 5e-2], tau=1.5), 15, 28,
+             ['x', 'px', ('NLK', 't0')], {'tau': 1.5})):
+        ring = lat('alba.mad')
+        ring.insert(0, kicker)
+        fl = ufo.FIVED | ufo.KICK | ufo.DOUBLE_PRECISION
+        tr = ufo.Track(ring, flags=fl, turns=turns, particles=n, parameters=params, where=[-1])
+        pool = np.zeros(tr.parameters.shape)
+        pool[:, 0] = rng.normal(size=n) * np.sqrt(0.5 * betax * ex0)
+        pool[:, 1] = rng.normal(size=n) * np.sqrt(0.5 * ex0 / betax)
+        if len(params) > 2:  # the trigger-time scan of the HOWTO, one t0 per 4 particles
+            pool[:, 2] = 5.0 + np.repeat(np.linspace(0., 1., 7, endpoint=False), 4)
+        tr.parameters[:] = pool
+        tr.run(threads=8)
+        add(name, 'track', ring, fl, dict(turns=turns, particles=n,
+                                          parameters=latjson.params_dump(params), where=[-1],
+                                          dp=0.0, kicker=type(kicker).__name__, **extra),
+            {'tracks': tr.tracks}, {'pool': pool})
+
     # --- closed orbit (reference: Nelder-Mead, 200 iterations)
     co_l = lat('alba.mad')
     co_l_d = {e.label: e for e in co_l.flatten()}

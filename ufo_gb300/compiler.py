@@ -33,15 +33,18 @@ import math
 import numpy as np
 
 from . import aperture as _ap
+from . import cexpr as _cx
 from . import crmath
 from . import elements as E
 from .flags import LINEAR, FIVED, EXACT, KICK, ACHROMATIC, YOSHIDA, FMA
 
 # ---- opcodes (shared with csrc/ufo_kernels.cuh and oracle) ----
 OP_NOP, OP_DRIFT, OP_KICK, OP_TEAPOT, OP_ALIGN, OP_EDGE, OP_THICKQ, OP_THICKB, OP_WIRE, \
-    OP_APERTURE, OP_OBSERVE = range(11)
+    OP_APERTURE, OP_OBSERVE, OP_DYNKICK = range(12)
 OP_NAMES = ['nop', 'drift', 'kick', 'teapot', 'align', 'edge', 'thickq', 'thickb', 'wire',
-            'aperture', 'observe']
+            'aperture', 'observe', 'dynkick']
+# deepest expression stack of a dynamic-kick coefficient (csrc/ops.cuh: eval_prog)
+DYN_STACK = 32
 
 # drift forms: 0 -> x + px*c0 ; 1 -> x + (px*c0)*c1 ; 2 -> x + (px*c0)/c1
 DF_MUL, DF_MUL2, DF_DIV = 0, 1, 2
@@ -119,6 +122,18 @@ class Val:
     def finite_nonzero_everywhere(self):
         a = np.asarray(self.v)
         return bool(np.all(a != 0.0))
+
+
+class Dyn:
+    """A value that the reference computed at run time from C text reading
+    the turn or the particle (a user ``method()`` override, e.g. the
+    time-gated kicker of HOWTO.md:84-200): a stack program whose PUSH values
+    are Vals over seeds (bound parameters resolved per seed)."""
+    __slots__ = ('code', 'text')
+
+    def __init__(self, code, text):
+        self.code = code
+        self.text = text
 
 
 def _fn(name, a):
@@ -547,11 +562,105 @@ class _Lowerer:
         self.emit(op)
 
 
-def _mp_list(lst, name):
+def _dyn_kick(lw, knl, ksl, elem):
+    """A thin kick some of whose coefficients are run-time expressions: the
+    reference's untrimmed Horner (methods.kick, ufo/methods.py:45-76, LINEAR
+    truncation included) with each coefficient evaluated per particle and
+    turn.  Table: for every coefficient, normal then skew, [n, (opcode,
+    value) x n]; a plain coefficient is the one-op program PUSH c."""
+    norm = KickSpec._trunc(list(knl), lw.flags)
+    skew = KickSpec._trunc(list(ksl), lw.flags)
+    if len(norm) > MAX_ORDERS or len(skew) > MAX_ORDERS:
+        raise NotImplementedError(f'more than {MAX_ORDERS} multipole orders')
+    consts = []
+    flops = 0
+    for c in norm + skew:
+        code = c.code if isinstance(c, Dyn) else [(_cx.PUSH, Val.of(c))]
+        consts.append(Val.of(float(len(code))))
+        for opc, v in code:
+            consts += [Val.of(float(opc)), Val.of(v)]
+            flops += opc in (_cx.ADD, _cx.SUB, _cx.MUL, _cx.DIV)
+    fl = F_ACHRO if lw.flags & ACHROMATIC else 0
+    op = Op(OP_DYNKICK, fl, ints=[len(norm), len(skew), len(consts)], consts=consts, elem=elem)
+    # the untrimmed kick: per order 4 mul + 2 add/sub + 2 div, plus the oodppo products
+    n_terms = sum(max(len(lst) - 1, 0) for lst in (norm, skew))
+    op.flops = op.flops_fast = flops + 8 * n_terms + (0 if fl else len(norm) + len(skew)) + \
+        2 * (len(norm) > 0) + 2 * (len(skew) > 0)
+    lw.emit(op)
+
+
+def _to_value(v, seed_values, name):
+    """One attribute value handed to a base-class method(): numbers become
+    Vals; C text becomes a Val when it reads neither the turn nor the particle
+    (folded per seed as the reference's compiler would compute it) and a Dyn
+    otherwise."""
+    if isinstance(v, (Val, Dyn)):
+        return v
+    if isinstance(v, str):
+        code, _, top = _cx.compile_expr(v, f'{name} = {v!r}', allow_params=True)
+        if top is not None:
+            raise NotImplementedError(
+                f'{name} = {v!r}: the reference pastes this text next to other operators, '
+                f'where C precedence regroups it; wrap it in parentheses')
+        if any(op == _cx.VAR and int(val) in (1, 3) for op, val in code):
+            raise NotImplementedError(f'{name} = {v!r}: px and py change within the kick')
+        if _cx.depth(code) > DYN_STACK:
+            raise NotImplementedError(f'{name} = {v!r}: expression too deep')
+        cols = [int(val) for op, val in code if op == _cx.PARAM]
+        for c in cols:
+            if c >= seed_values.shape[1]:
+                raise IndexError(f'{name} = {v!r}: parameters[{c}] outside the parameter list')
+        if _cx.is_constant(code):
+            vals = np.array([_cx.evaluate(code, params=row, correctly_rounded=not cols)
+                             for row in seed_values])
+            return Val(vals if cols else np.float64(vals[0]), not cols)
+        prog = [(_cx.PUSH, Val(seed_values[:, int(val)].copy(), False)) if op == _cx.PARAM
+                else (op, Val.of(val)) for op, val in code]
+        return Dyn(prog, v)
+    if isinstance(v, (list, tuple)):
+        return [_to_value(x, seed_values, f'{name}[{i}]') for i, x in enumerate(v)]
+    return Val.of(float(v))
+
+
+def _user_method(elem, idx, cols, seed_values, flags, where):
+    """Run an element's own ``method()`` override the way ufo/lattice.py:107-113
+    calls it (bound parameters as the text ``parameters[i]``, plus flags and
+    fracture) and return the attribute values it handed to its base class."""
+    tokens = {name: f'parameters[{col}]' for name, col in cols.items()}
+    out = elem.method(flags=flags, fracture=list(where), **tokens)
+    passes = [p for p in (out if isinstance(out, (list, tuple)) else [out])
+              if isinstance(p, E.PassMethod)]
+    if len(passes) != 1 or passes[0].element is not elem:
+        raise NotImplementedError(
+            f'{elem.label}: method() must return its base class method() result; user '
+            f'OpenCL pass methods cannot run in the data-driven GPU kernels')
+    prm = {}
+    for name, v in passes[0].values.items():
+        if name in ('flags', 'fracture') or v is None:
+            continue
+        prm[name] = _to_value(v, seed_values, f'{elem.label}.{name}')
+    return prm
+
+
+def _has_dyn(v):
+    if isinstance(v, Dyn):
+        return True
+    if isinstance(v, list):
+        return any(_has_dyn(x) for x in v)
+    return False
+
+
+def _mp_list(lst, name, seed_values=None):
     if isinstance(lst, str) or isinstance(lst, Val):
         raise NotImplementedError(f'{name} cannot be a parameter as a whole vector; '
                                   f'use the scalar names (e.g. dk2, k3s)')
-    return [Val.of(v) for v in lst]
+    out = []
+    for i, v in enumerate(lst):
+        if isinstance(v, str):  # C text in the lattice itself, pasted by the reference
+            v = _to_value(v, seed_values if seed_values is not None else np.zeros((1, 1)),
+                          f'{name}[{i}]')
+        out.append(v if isinstance(v, Dyn) else Val.of(v))
+    return out
 
 
 def _dk_from_kwargs(kwargs, dkn, dks):
@@ -576,16 +685,22 @@ def _resolve(elem, prm, name, default=None):
                   getattr(elem, name, default))
 
 
-def lower_element(lw, elem, idx, prm, where):
+def lower_element(lw, elem, idx, prm, where, cols=None, seed_values=None):
     """Lower one flat element.  ``prm`` maps attribute name -> Val (bound
-    parameters); ``where`` is its fracture list (fractions in [0, 1)).
-    Returns the number of code chunks emitted (segments = chunks - 1)."""
+    parameters); ``where`` is its fracture list (fractions in [0, 1)).  An
+    element whose class overrides ``method()`` is lowered from the values its
+    override hands to the base class (``cols``: attribute -> parameter column,
+    ``seed_values``: the per-seed parameter rows)."""
     flags = lw.flags
     if type(elem).method is not E.Element.method:
-        raise NotImplementedError(
-            f'{elem.label}: element overrides method(); user OpenCL pass methods cannot run '
-            f'in the data-driven GPU kernels')
+        if seed_values is None:
+            seed_values = np.zeros((lw.S, 1))
+        prm = _user_method(elem, idx, cols or {}, seed_values, flags, where)
     kind = elem.kind
+    if kind != 'multipole' and any(_has_dyn(v) for v in prm.values()):
+        raise NotImplementedError(
+            f'{elem.label}: values that depend on the turn or the particle are supported for '
+            f'thin multipole coefficients (knl, ksl, kN, kNs) only')
     pieces = []
     f0 = 0.0
     for f in list(where) + [1.0]:
@@ -613,8 +728,8 @@ def lower_element(lw, elem, idx, prm, where):
         chunks(lambda fr: lw.drift(DF_MUL2, L, fr, elem=idx))
         return
     if kind == 'multipole':
-        knl = _mp_list(elem.knl, 'knl') if 'knl' not in prm else _mp_list(prm['knl'], 'knl')
-        ksl = _mp_list(elem.ksl, 'ksl') if 'ksl' not in prm else _mp_list(prm['ksl'], 'ksl')
+        knl = _mp_list(prm['knl'] if 'knl' in prm else elem.knl, 'knl', seed_values)
+        ksl = _mp_list(prm['ksl'] if 'ksl' in prm else elem.ksl, 'ksl', seed_values)
         dx = _resolve(elem, prm, 'dx')
         dy = _resolve(elem, prm, 'dy')
         for p, v in prm.items():
@@ -622,8 +737,13 @@ def lower_element(lw, elem, idx, prm, where):
                 knl[int(p[1:])] = v
             if p[:1] == 'k' and p[-1:] == 's' and p[1:-1].isdigit():
                 ksl[int(p[1:-1])] = v
+        if _has_dyn(dx) or _has_dyn(dy):
+            raise NotImplementedError(f'{elem.label}: turn-dependent offsets')
         lw.align(dx, dy, idx)
-        lw.kick(knl, ksl, idx)
+        if _has_dyn(knl) or _has_dyn(ksl):
+            _dyn_kick(lw, knl, ksl, idx)
+        else:
+            lw.kick(knl, ksl, idx)
         lw.align(-dx, -dy, idx)
         return
     if kind == 'wire':
@@ -886,7 +1006,7 @@ def compile_line(line, flags=0, parameters=(), where=(), seed_values=None, count
         if pre[idx]:
             lw.new_segment()
         prm = {name: Val(seed_values[:, col].copy(), False) for name, col in binds[idx].items()}
-        lower_element(lw, elem, idx, prm, per[idx])
+        lower_element(lw, elem, idx, prm, per[idx], binds[idx], seed_values)
     if flags & FMA:
         lw.segments = [_merge_drifts(seg) for seg in lw.segments]
     if dump_end is None:

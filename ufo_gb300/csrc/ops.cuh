@@ -17,7 +17,7 @@ namespace ufo {
 
 enum : int {
   OP_NOP = 0, OP_DRIFT, OP_KICK, OP_TEAPOT, OP_ALIGN, OP_EDGE, OP_THICKQ, OP_THICKB, OP_WIRE,
-  OP_APERTURE, OP_OBSERVE
+  OP_APERTURE, OP_OBSERVE, OP_DYNKICK
 };
 enum : int { DF_MUL = 0, DF_MUL2 = 1, DF_DIV = 2 };
 enum : int {
@@ -144,15 +144,11 @@ UFO_DEV int drift_nconst(int form, bool exact) {
 //   px -= b; py += a
 // `c` holds the structurally non-zero coefficients in ascending order.
 
-// untrimmed evaluation (reference semantics incl. 0*x terms) for non-finite x/y
-template <bool SKEW>
-UFO_DEV void horner_full(const State &s, int n, uint32_t mask, const double *c, bool achro,
-                         double &pxd, double &pyd) {
-  // coefficient j: its value if bit j is set, else a literal 0.
-  auto coef = [&](int j) -> double {
-    if (!((mask >> j) & 1u)) return 0.0;
-    return ld(c + __popc(mask & ((1u << j) - 1u)));
-  };
+// untrimmed evaluation (reference semantics incl. 0*x terms): `coef(j)` gives
+// coefficient j of the list
+template <bool SKEW, class Coef>
+UFO_DEV void horner_any(const State &s, int n, Coef coef, bool achro, double &pxd,
+                        double &pyd) {
   double a = achro ? coef(n - 1) : mul(coef(n - 1), s.o);
   double b = 0.0;
   for (int order = n - 1; order > 0; --order) {
@@ -174,6 +170,17 @@ UFO_DEV void horner_full(const State &s, int n, uint32_t mask, const double *c, 
     pxd = b;
     pyd = a;
   }
+}
+
+// the untrimmed kick on table coefficients (non-finite x/y): coefficient j is
+// its value if bit j of the mask is set, else a literal 0.
+template <bool SKEW>
+UFO_DEV void horner_full(const State &s, int n, uint32_t mask, const double *c, bool achro,
+                         double &pxd, double &pyd) {
+  horner_any<SKEW>(s, n, [&](int j) -> double {
+    if (!((mask >> j) & 1u)) return 0.0;
+    return ld(c + __popc(mask & ((1u << j) - 1u)));
+  }, achro, pxd, pyd);
 }
 
 // trimmed evaluation: za/zb mark exact (structural) zeros
@@ -853,19 +860,25 @@ UFO_DEV void wire(State &s, const double *c) {
   s.py = add(s.py, mul(B, sa));
 }
 
-// ---------------------------------------------------------------- aperture
-// stack program of ``{window} == 0`` (ufo_gb300/aperture.py); table holds
-// (opcode, value) pairs.  Returns true when the particle is lost.
-UFO_DEV bool aperture_lost(const State &s, const double *c, int n) {
-  double st[16];
+// ---------------------------------------------------------------- expressions
+// stack programs of C expressions (ufo_gb300/cexpr.py): the table holds
+// (opcode, value) pairs.  Opcodes 3,4,19,20,22-28 are unary, 21 is ?:, 1 and 2
+// push a literal or a variable, the rest are binary.
+UFO_DEV bool prog_unary(int op) { return op == 3 || op == 4 || op == 19 || op == 20 ||
+                                         (op >= 22 && op <= 28); }
+
+// value of a program in `out`; false (and `out` untouched) when the program
+// would leave its stack of DEPTH slots
+template <int DEPTH>
+UFO_DEV bool eval_prog(const State &s, const double *c, int n, double &out) {
+  double st[DEPTH];
   int sp = 0;
   for (int i = 0; i < n; ++i) {
     const int op = static_cast<int>(ld(c + 2 * i));
     const double v = ld(c + 2 * i + 1);
     // depth guards: a malformed program stops instead of leaving the stack
-    const int need = (op == 1 || op == 2) ? 0 : (op == 3 || op == 4 || op == 19 || op == 20) ? 1
-                   : op == 21 ? 3 : 2;
-    if (sp < need || ((op == 1 || op == 2) && sp >= 16)) return false;
+    const int need = (op == 1 || op == 2) ? 0 : prog_unary(op) ? 1 : op == 21 ? 3 : 2;
+    if (sp < need || ((op == 1 || op == 2) && sp >= DEPTH)) return false;
     if (op == 1) { st[sp++] = v; continue; }
     if (op == 2) {
       const int k = static_cast<int>(v);
@@ -873,10 +886,25 @@ UFO_DEV bool aperture_lost(const State &s, const double *c, int n) {
                : k == 5 ? s.dp : k == 6 ? s.o : static_cast<double>(s.turn);
       continue;
     }
-    if (op == 3) { st[sp - 1] = -st[sp - 1]; continue; }
-    if (op == 4) { st[sp - 1] = st[sp - 1] == 0 ? 1. : 0.; continue; }
-    if (op == 19) { st[sp - 1] = fabs(st[sp - 1]); continue; }
-    if (op == 20) { st[sp - 1] = __dsqrt_rn(st[sp - 1]); continue; }
+    if (prog_unary(op)) {
+      const double a = st[sp - 1];
+      double r;
+      switch (op) {
+        case 3: r = -a; break;
+        case 4: r = a == 0 ? 1. : 0.; break;
+        case 19: r = fabs(a); break;
+        case 20: r = __dsqrt_rn(a); break;
+        case 22: r = sin(a); break;
+        case 23: r = cos(a); break;
+        case 24: r = tan(a); break;
+        case 25: r = exp(a); break;
+        case 26: r = log(a); break;
+        case 27: r = static_cast<double>(__double2float_rn(a)); break;  // (float)
+        default: r = trunc(a); break;                                   // (int)
+      }
+      st[sp - 1] = r;
+      continue;
+    }
     if (op == 21) {
       const double b = st[--sp], a = st[--sp], cc = st[--sp];
       st[sp++] = cc != 0 ? a : b;
@@ -902,7 +930,15 @@ UFO_DEV bool aperture_lost(const State &s, const double *c, int n) {
     }
     st[sp++] = r;
   }
-  return sp > 0 && st[sp - 1] != 0;
+  if (sp < 1) return false;
+  out = st[sp - 1];
+  return true;
+}
+
+// ``{window} == 0`` of an aperture (ufo_gb300/aperture.py): true when lost
+UFO_DEV bool aperture_lost(const State &s, const double *c, int n) {
+  double v;
+  return eval_prog<16>(s, c, n, v) && v != 0;
 }
 
 UFO_DEV void align(State &s, int flags, const double *c) {
@@ -957,6 +993,47 @@ __device__ __noinline__ bool aperture_ool(double x, double px, double y, double 
   State s{};
   s.x = x; s.px = px; s.y = y; s.py = py; s.z = z; s.dp = dp; s.o = o; s.turn = turn;
   return aperture_lost(s, c, n);
+}
+
+// A thin kick whose coefficients are programs (a user pass method's C text,
+// ufo_gb300/compiler.py: _dyn_kick): table [n, (opcode, value) x n] per
+// coefficient, normal then skew, `words` entries in all.  The reference's
+// untrimmed Horner in its operation order (methods.kick, ufo/methods.py:45-76)
+// in both arithmetic modes.  Every read stays within the op's `words` table
+// entries; a malformed program yields a NaN coefficient.
+__device__ __noinline__ PxPy dynkick_ool(double x, double px, double y, double py, double z,
+                                         double dp, double o, int turn, int nn, int ns,
+                                         bool achro, int words, const double *c) {
+  State s{};
+  s.x = x; s.px = px; s.y = y; s.py = py; s.z = z; s.dp = dp; s.o = o; s.turn = turn;
+  auto coef = [&](int j) -> double {
+    double v = __longlong_as_double(0x7ff8000000000000ll);
+    int q = 0;
+    for (int k = 0; k <= j; ++k) {
+      if (q >= words) return v;
+      const double len = ld(c + q);
+      if (!(len >= 1.0 && len <= 0.5 * (words - q - 1))) return v;
+      if (k == j) {
+        eval_prog<32>(s, c + q + 1, static_cast<int>(len), v);
+        return v;
+      }
+      q += 1 + 2 * static_cast<int>(len);
+    }
+    return v;
+  };
+  if (nn) {
+    double a, b;
+    horner_any<false>(s, nn, coef, achro, a, b);
+    s.px = sub(s.px, a);
+    s.py = add(s.py, b);
+  }
+  if (ns) {
+    double a, b;
+    horner_any<true>(s, ns, [&](int j) { return coef(nn + j); }, achro, a, b);
+    s.px = sub(s.px, a);
+    s.py = add(s.py, b);
+  }
+  return {s.px, s.py};
 }
 
 __device__ __noinline__ PxPy edge_ool(double x, double y, double px, double py, double o,

@@ -155,6 +155,14 @@ UFO_DEV void one_turn(State &s, const TrackArgs &a, const double *tab, int64_t p
       case OP_OBSERVE:
         observe(s, a, p, op.i0);
         break;
+      case OP_DYNKICK:
+        if (FULL) {
+          const PxPy r = dynkick_ool(s.x, s.px, s.y, s.py, s.z, s.dp, s.o, s.turn, op.i0, op.i1,
+                                     op.flags & F_ACHRO, op.i2, c);
+          s.px = r.px;
+          s.py = r.py;
+        }
+        break;
       default:
         break;
     }
@@ -510,26 +518,30 @@ int64_t op_consts(const int32_t *w) {
     case ufo::OP_APERTURE:
       if (flags & ufo::F_CIRCLE) return 1;
       return w[3] >= 0 ? 2 * static_cast<int64_t>(w[3]) : -1;
+    case ufo::OP_DYNKICK:
+      if (w[3] < 0 || w[4] < 0 || w[3] > 32 || w[4] > 32 || w[5] < w[3] + w[4]) return -1;
+      return w[5];
     default:
       return -1;
   }
 }
 
-// simulate an aperture stack program (row 0 of the table): every pop must
-// find an operand and the depth must stay within the kernels' 16 slots
-bool aperture_ok(const double *prog, int n) {
+// simulate an expression stack program (row 0 of the table; the opcodes are
+// the same in every row): every pop must find an operand and the depth must
+// stay within the kernel's `depth` slots
+bool prog_ok(const double *prog, int n, int depth) {
   int sp = 0;
   for (int i = 0; i < n; ++i) {
     const double code = prog[2 * i];
-    if (!(code >= 1 && code <= 21) || code != static_cast<int>(code)) return false;
+    if (!(code >= 1 && code <= 28) || code != static_cast<int>(code)) return false;
     const int op = static_cast<int>(code);
     if (op == 2) {
       const double v = prog[2 * i + 1];
       if (!(v >= 0 && v <= 7)) return false;
     }
     if (op == 1 || op == 2) {
-      if (++sp > 16) return false;
-    } else if (op == 3 || op == 4 || op == 19 || op == 20) {
+      if (++sp > depth) return false;
+    } else if (op == 3 || op == 4 || op == 19 || op == 20 || (op >= 22 && op <= 28)) {
       if (sp < 1) return false;
     } else if (op == 21) {
       if (sp < 3) return false;
@@ -542,6 +554,23 @@ bool aperture_ok(const double *prog, int n) {
   return n == 0 || sp >= 1;
 }
 
+bool aperture_ok(const double *prog, int n) { return prog_ok(prog, n, 16); }
+
+// the coefficient programs of a dynamic kick: n_coef of them, exactly filling
+// `words` table entries, each a valid program of at least one op
+bool dynkick_ok(const double *c, int n_coef, int64_t words) {
+  int64_t q = 0;
+  for (int j = 0; j < n_coef; ++j) {
+    if (q >= words) return false;
+    const double len = c[q];
+    if (!(len >= 1 && len <= 4096) || len != static_cast<int>(len)) return false;
+    const int n = static_cast<int>(len);
+    if (q + 1 + 2 * n > words || !prog_ok(c + q + 1, n, 32)) return false;
+    q += 1 + 2 * n;
+  }
+  return q == words;
+}
+
 // ops the lean interpreter does not carry
 bool needs_full(const int32_t *ops, int n_ops) {
   for (int i = 0; i < n_ops; ++i) {
@@ -551,6 +580,7 @@ bool needs_full(const int32_t *ops, int n_ops) {
     if ((kind == ufo::OP_DRIFT || kind == ufo::OP_TEAPOT) && (flags & ufo::F_EXACT)) return true;
     if (kind == ufo::OP_EDGE && (flags & ufo::F_RTPSI)) return true;
     if (kind == ufo::OP_APERTURE && !(flags & ufo::F_CIRCLE)) return true;
+    if (kind == ufo::OP_DYNKICK) return true;
   }
   return false;
 }
@@ -558,7 +588,7 @@ bool needs_full(const int32_t *ops, int n_ops) {
 int validate_ops(const int32_t *ops, int n_ops, int64_t stride, const double *table) {
   for (int i = 0; i < n_ops; ++i) {
     const int32_t *w = ops + i * UFO_OP_WORDS;
-    if (w[0] < ufo::OP_NOP || w[0] > ufo::OP_OBSERVE)
+    if (w[0] < ufo::OP_NOP || w[0] > ufo::OP_DYNKICK)
       return fail(UFO_E_ARG, "op %d: unknown kind %d", i, w[0]);
     const int64_t nc = op_consts(w);
     if (nc < 0) return fail(UFO_E_ARG, "op %d (kind %d): invalid shape", i, w[0]);
@@ -568,6 +598,8 @@ int validate_ops(const int32_t *ops, int n_ops, int64_t stride, const double *ta
     if (w[0] == ufo::OP_APERTURE && !(w[1] & ufo::F_CIRCLE) && table &&
         !aperture_ok(table + w[2], w[3]))
       return fail(UFO_E_ARG, "op %d: malformed aperture program", i);
+    if (w[0] == ufo::OP_DYNKICK && table && !dynkick_ok(table + w[2], w[3] + w[4], w[5]))
+      return fail(UFO_E_ARG, "op %d: malformed dynamic-kick programs", i);
   }
   return UFO_OK;
 }

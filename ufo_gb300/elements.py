@@ -36,10 +36,21 @@ def _dk_index(name, prefix):
     return None
 
 
+class PassMethod:
+    """What ``Element.method()`` returns: the element and the attribute values
+    its pass method was called with."""
+    __slots__ = ('element', 'values')
+
+    def __init__(self, element, values):
+        self.element = element
+        self.values = values
+
+
 class Element:
-    """Base element.  ``lower()`` is what the compiler calls; subclasses that
-    override ``method()`` (the reference's OpenCL-string plugin point) cannot
-    run in the data-driven kernels and are rejected by the compiler."""
+    """Base element.  ``lower()`` is what the compiler calls.  Subclasses may
+    override ``method()`` (the reference's plugin point) as long as they return
+    their base class's ``method()`` result; the values they pass it may be C
+    expressions (see ``method``)."""
 
     kind = 'element'
 
@@ -66,10 +77,17 @@ class Element:
             return (self.dks if skew else self.dkn)[order]
         raise AttributeError(name)
 
-    def method(self, **kwargs):
-        """The reference's plugin point returned OpenCL source; this build has
-        no source generation.  Kept so that subclass detection works."""
-        return ['']
+    def method(self, flags=0, fracture=None, **kwargs):
+        """The reference's plugin point (ufo/elements.py), which returned
+        OpenCL source.  Here it returns ``[PassMethod(self, values)]``: a
+        subclass overriding it (a time-dependent kicker, HOWTO.md:84-200) calls
+        ``super().method(k1='(C expression)', **kwargs)`` as it would with the
+        reference, and the compiler lowers the values it passed (numbers, or C
+        expressions of ``turn``, the coordinates and ``parameters[i]``)."""
+        values = dict(kwargs)
+        values['flags'] = flags
+        values['fracture'] = fracture
+        return [PassMethod(self, values)]
 
     def lower(self):
         """Return a dict of resolved attributes for the compiler."""
