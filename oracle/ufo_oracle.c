@@ -244,7 +244,7 @@ static double eval_(const state *s, const double *prog, int n) {
         case 25: st[sp - 1] = exp(st[sp - 1]); break;
         case 26: st[sp - 1] = log(st[sp - 1]); break;
         case 27: st[sp - 1] = (double)(float)st[sp - 1]; break;
-        case 28: st[sp - 1] = trunc(st[sp - 1]); break;
+        case 28: st[sp - 1] = trunc(st[sp - 1]) + 0.0; break;  /* (int): no -0 */
         case 21: b = st[--sp]; a = st[--sp]; c = st[--sp]; st[sp++] = c != 0 ? a : b; break;
         default:
             b = st[--sp];
@@ -255,7 +255,7 @@ static double eval_(const state *s, const double *prog, int n) {
             case 7: c = a * b; break;
             case 8: c = a / b; break;
             case 9: c = b != 0 ? (double)(long long)(a / b) : NAN; break;
-            case 10: c = b != 0 ? fmod(a, b) : NAN; break;
+            case 10: c = b != 0 ? fmod(a, b) + 0.0 : NAN; break;
             case 11: c = a < b; break;
             case 12: c = a <= b; break;
             case 13: c = a > b; break;

@@ -144,3 +144,91 @@ def test_oracle_reproduces_reference_kickers():
         c = H.case(name)
         out = H.oracle_case(c)
         assert np.array_equal(out['tracks'], H.arr(name, 'out/tracks'), equal_nan=True)
+
+
+def _random_expr(rng, depth):
+    """A random expression of the grammar, free of C undefined behaviour:
+    integer arithmetic only between small leaves, integer division and % only
+    by non-zero literals, (int) casts only of bounded values.  Returns
+    (text, type, is_leaf)."""
+    if depth == 0 or rng.random() < 0.25:
+        k = rng.integers(7)
+        if k == 0:
+            return str(int(rng.integers(1, 10))), 'i', True
+        if k == 1:
+            return repr(float(rng.normal())), 'd', True
+        if k == 2:
+            return f'{rng.random():.6f}f', 'f', True
+        if k == 3:
+            return 'turn', 'i', True
+        if k == 4:
+            return f'parameters[{int(rng.integers(2))}]', 'd', True
+        return str(rng.choice(['x', 'px', 'y', 'dp', 'oodppo'])), 'd', True
+    k = rng.integers(9)
+    a, ta, la = _random_expr(rng, depth - 1)
+    if k == 0:
+        op = str(rng.choice(['-', '!']))
+        return f'{op}({a})', ('i' if op == '!' else ta), False
+    if k == 1:
+        c = str(rng.choice(['float', 'double']))
+        return f'({c})({a})', c[0], False
+    if k == 2:  # bounded integer cast
+        return f'(int)(fabs({a}) < 1e6 ? ({a}) : 0.)', 'i', False
+    if k == 3:
+        f = str(rng.choice(['fabs', 'sin', 'cos', 'exp', 'sqrt', 'log']))
+        arg = f'fabs({a})' if f in ('sqrt', 'log') else a
+        return f'{f}({arg})', 'd', False
+    b, tb, lb = _random_expr(rng, depth - 1)
+    if k == 4:
+        c, _, _ = _random_expr(rng, depth - 1)
+        return f'(({c}) ? ({a}) : ({b}))', max(ta, tb, key='ifd'.index), False
+    if k == 5:
+        op = str(rng.choice(['<', '<=', '>', '>=', '==', '!=', '&&', '||']))
+        return f'(({a}) {op} ({b}))', 'i', False
+    op = str(rng.choice(['+', '-', '*', '/']))
+    if ta == 'i' and tb == 'i':
+        if op == '/' or not (la and lb):
+            # integer division by a non-zero literal, or mix in a double
+            return (f'(({a}) / {int(rng.integers(1, 10))})' if op == '/' and la
+                    else f'(({a}) {op} (({b}) * 1.5))'), 'd' if op != '/' or not la else 'i', False
+        return f'({a} {op} {b})', 'i', False
+    if op == '%':
+        op = '+'
+    t = max(ta, tb, key='ifd'.index)
+    return f'(({a}) {op} ({b}))', t, False
+
+
+def test_random_expressions_match_c():
+    """400 random expressions (seeded), each compiled by gcc and by the
+    expression compiler, evaluated at 8 points: bit-identical values."""
+    from ufo_gb300 import cexpr as X
+    rng = np.random.default_rng(11)
+    exprs = [_random_expr(rng, 4)[0] for _ in range(400)]
+    src = ['#include <math.h>']
+    for i, e in enumerate(exprs):
+        src.append(f'double g{i}(int turn, double x, double px, double y, double py, double z, '
+                   f'double dp, double oodppo, const double *parameters) '
+                   f'{{ return (double)({e}); }}')
+    d = tempfile.mkdtemp()
+    c, so = os.path.join(d, 'r.c'), os.path.join(d, 'r.so')
+    with open(c, 'w') as f:
+        f.write('\n'.join(src) + '\n')
+    subprocess.run(['gcc', '-O0', '-ffp-contract=off', '-fno-fast-math', '-w', '-shared', '-fPIC',
+                    '-o', so, c, '-lm'], check=True)
+    lib = ctypes.CDLL(so)
+    pts = []
+    for _ in range(8):
+        v = rng.normal(size=6) * [1e-2, 1e-3, 1e-2, 1e-3, 0, 1e-3]
+        pts.append((int(rng.integers(1, 40)), *v, 1.0 / (1.0 + v[5]),
+                    np.array([5.0 + rng.random(), rng.normal()])))
+    for i, e in enumerate(exprs):
+        fn = getattr(lib, f'g{i}')
+        fn.restype = ctypes.c_double
+        fn.argtypes = [ctypes.c_int] + [ctypes.c_double] * 7 + [ctypes.POINTER(ctypes.c_double)]
+        code, _, _ = X.compile_expr(e, allow_params=True)
+        for turn, x, px, y, py, z, dp, o, prm in pts:
+            want = fn(turn, x, px, y, py, z, dp, o,
+                      prm.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+            got = X.evaluate(code, (x, px, y, py, z, dp, o, turn), prm)
+            assert np.float64(got).tobytes() == np.float64(want).tobytes() or \
+                (np.isnan(got) and np.isnan(want)), (e, turn, got, want)

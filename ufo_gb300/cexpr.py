@@ -17,7 +17,9 @@ i-th column of the parameter list, resolved per seed by the compiler),
 sin cos tan exp log``.
 
 Typing follows C: operands of a binary operator convert to the wider of int,
-float and double; int/int divides with truncation and ``%`` takes ints; a float
+float and double; int/int divides with truncation and ``%`` takes ints; integer
+results are never -0 (``0 - a`` for negation, ``+ 0`` after products,
+truncation and remainders); a float
 result is rounded to float32 (emitted as an explicit F32 op, so the FP64
 evaluators reproduce float arithmetic exactly: a double result of two floats
 rounds once to the correctly rounded float).  Calls take and return double
@@ -165,6 +167,8 @@ class Parser:
                 self.code.append((IDIV if to == 'i' else DIV, 0.0))
             else:
                 self.code.append(({'+': ADD, '-': SUB, '*': MUL}[op], 0.0))
+                if op == '*' and to == 'i':  # 0 * -n is 0, not -0
+                    self.code += [(PUSH, 0.0), (ADD, 0.0)]
             if to == 'f':
                 self.code.append((F32, 0.0))
             left = to
@@ -173,8 +177,12 @@ class Parser:
         tok = self.peek()
         if tok[0] == 'op' and tok[1] in ('-', '+', '!'):
             op = self.take()[1]
+            start = len(self.code)
             t = self.unary()
-            if op == '-':
+            if op == '-' and t == 'i':  # ints have no -0: 0 - a
+                self.code.insert(start, (PUSH, 0.0))
+                self.code.append((SUB, 0.0))
+            elif op == '-':
                 self.code.append((NEG, 0.0))
             elif op == '!':
                 self.code.append((NOT, 0.0))
@@ -358,7 +366,7 @@ def evaluate(code, vars=(0., 0., 0., 0., 0., 0., 1., 0), params=(), correctly_ro
                 elif op == IDIV:
                     r = float(math.trunc(a / b)) if b != 0 else math.nan
                 elif op == IMOD:
-                    r = float(math.fmod(a, b)) if b != 0 else math.nan
+                    r = float(math.fmod(a, b)) + 0.0 if b != 0 else math.nan
                 elif op == LT:
                     r = float(a < b)
                 elif op == LE:

@@ -900,7 +900,7 @@ UFO_DEV bool eval_prog(const State &s, const double *c, int n, double &out) {
         case 25: r = exp(a); break;
         case 26: r = log(a); break;
         case 27: r = static_cast<double>(__double2float_rn(a)); break;  // (float)
-        default: r = trunc(a); break;                                   // (int)
+        default: r = add(trunc(a), 0.0); break;                         // (int): no -0
       }
       st[sp - 1] = r;
       continue;
@@ -917,8 +917,11 @@ UFO_DEV bool eval_prog(const State &s, const double *c, int n, double &out) {
       case 6: r = sub(a, b); break;
       case 7: r = mul(a, b); break;
       case 8: r = dvd(a, b); break;
-      case 9: r = b != 0 ? trunc(dvd(a, b)) : __longlong_as_double(0x7ff8000000000000ll); break;
-      case 10: r = b != 0 ? fmod(a, b) : __longlong_as_double(0x7ff8000000000000ll); break;
+      // integer / and %: truncated, and never -0 (C ints have none)
+      case 9: r = b != 0 ? add(trunc(dvd(a, b)), 0.0) : __longlong_as_double(0x7ff8000000000000ll);
+        break;
+      case 10: r = b != 0 ? add(fmod(a, b), 0.0) : __longlong_as_double(0x7ff8000000000000ll);
+        break;
       case 11: r = a < b; break;
       case 12: r = a <= b; break;
       case 13: r = a > b; break;
