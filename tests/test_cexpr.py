@@ -232,3 +232,31 @@ def test_random_expressions_match_c():
             got = X.evaluate(code, (x, px, y, py, z, dp, o, turn), prm)
             assert np.float64(got).tobytes() == np.float64(want).tobytes() or \
                 (np.isnan(got) and np.isnan(want)), (e, turn, got, want)
+
+
+def test_turn_outside_tracking_kernels_rejected():
+    """The reference's closed-orbit and optics kernels declare no ``turn``:
+    element text that reads it cannot build there, and is refused here."""
+    import kickers
+    import ufo_gb300 as u
+    from ufo_gb300 import compiler as C, drivers
+    gate = C.compile_line(u.Line('L', [kickers.NLKGate('N', knl=[0., 1e-3])]), u.KICK, [], [-1])
+    window = C.compile_line(u.Line('L', [u.Aperture('A', window='turn < 5 || x*x < 1e-4')]),
+                            u.KICK, [], [-1])
+    circle = C.compile_line(u.Line('L', [u.Aperture('A', window='x*x + y*y < 1e-4')]),
+                            u.KICK, [], [-1])
+    assert C.reads_turn(gate) and C.reads_turn(window) and not C.reads_turn(circle)
+    with pytest.raises(RuntimeError, match='turn'):
+        drivers._no_turn(gate, 'closed-orbit')
+    drivers._no_turn(circle, 'optics')
+
+
+def test_coordinate_columns_are_not_lattice_values():
+    import ufo_gb300 as u
+    from ufo_gb300 import compiler as C
+
+    class K(u.Multipole):
+        def method(self, **kwargs):
+            return super().method(k1='((turn > 2) ? parameters[0] : 0.)', **kwargs)
+    with pytest.raises(NotImplementedError, match='particle coordinate'):
+        C.compile_line(u.Line('L', [K('K', knl=[0., 1.])]), u.KICK, ['x', ('K', 'dx')], [-1])

@@ -589,7 +589,7 @@ def _dyn_kick(lw, knl, ksl, elem):
     lw.emit(op)
 
 
-def _to_value(v, seed_values, name):
+def _to_value(v, seed_values, name, coord_cols=()):
     """One attribute value handed to a base-class method(): numbers become
     Vals; C text becomes a Val when it reads neither the turn nor the particle
     (folded per seed as the reference's compiler would compute it) and a Dyn
@@ -610,6 +610,9 @@ def _to_value(v, seed_values, name):
         for c in cols:
             if c >= seed_values.shape[1]:
                 raise IndexError(f'{name} = {v!r}: parameters[{c}] outside the parameter list')
+            if c in coord_cols:
+                raise NotImplementedError(f'{name} = {v!r}: parameters[{c}] is a particle '
+                                          f'coordinate, not a lattice value')
         if _cx.is_constant(code):
             vals = np.array([_cx.evaluate(code, params=row, correctly_rounded=not cols)
                              for row in seed_values])
@@ -618,11 +621,11 @@ def _to_value(v, seed_values, name):
                 else (op, Val.of(val)) for op, val in code]
         return Dyn(prog, v)
     if isinstance(v, (list, tuple)):
-        return [_to_value(x, seed_values, f'{name}[{i}]') for i, x in enumerate(v)]
+        return [_to_value(x, seed_values, f'{name}[{i}]', coord_cols) for i, x in enumerate(v)]
     return Val.of(float(v))
 
 
-def _user_method(elem, idx, cols, seed_values, flags, where):
+def _user_method(elem, idx, cols, seed_values, flags, where, coord_cols=()):
     """Run an element's own ``method()`` override the way ufo/lattice.py:107-113
     calls it (bound parameters as the text ``parameters[i]``, plus flags and
     fracture) and return the attribute values it handed to its base class."""
@@ -638,8 +641,32 @@ def _user_method(elem, idx, cols, seed_values, flags, where):
     for name, v in passes[0].values.items():
         if name in ('flags', 'fracture') or v is None:
             continue
-        prm[name] = _to_value(v, seed_values, f'{elem.label}.{name}')
+        prm[name] = _to_value(v, seed_values, f'{elem.label}.{name}', coord_cols)
     return prm
+
+
+def reads_turn(prog):
+    """True when an aperture window or a dynamic-kick coefficient of the
+    compiled program reads ``turn`` (only the Track and StableAperture kernels
+    of the reference define it)."""
+    T = prog.table[0]
+    for row in prog.ops:
+        kind, fl, off = int(row[0]), int(row[1]), int(row[2])
+        if kind == OP_APERTURE and not fl & F_CIRCLE:
+            progs = [(off, int(row[3]))]
+        elif kind == OP_DYNKICK:
+            progs, q = [], off
+            while q < off + int(row[5]):
+                n = int(T[q])
+                progs.append((q + 1, n))
+                q += 1 + 2 * n
+        else:
+            continue
+        for start, n in progs:
+            codes = T[start:start + 2 * n].reshape(n, 2)
+            if np.any((codes[:, 0] == _cx.VAR) & (codes[:, 1] == _cx.VARS['turn'])):
+                return True
+    return False
 
 
 def _has_dyn(v):
@@ -685,7 +712,7 @@ def _resolve(elem, prm, name, default=None):
                   getattr(elem, name, default))
 
 
-def lower_element(lw, elem, idx, prm, where, cols=None, seed_values=None):
+def lower_element(lw, elem, idx, prm, where, cols=None, seed_values=None, coord_cols=()):
     """Lower one flat element.  ``prm`` maps attribute name -> Val (bound
     parameters); ``where`` is its fracture list (fractions in [0, 1)).  An
     element whose class overrides ``method()`` is lowered from the values its
@@ -695,7 +722,7 @@ def lower_element(lw, elem, idx, prm, where, cols=None, seed_values=None):
     if type(elem).method is not E.Element.method:
         if seed_values is None:
             seed_values = np.zeros((lw.S, 1))
-        prm = _user_method(elem, idx, cols or {}, seed_values, flags, where)
+        prm = _user_method(elem, idx, cols or {}, seed_values, flags, where, coord_cols)
     kind = elem.kind
     if kind != 'multipole' and any(_has_dyn(v) for v in prm.values()):
         raise NotImplementedError(
@@ -1001,12 +1028,13 @@ def compile_line(line, flags=0, parameters=(), where=(), seed_values=None, count
     S = seed_values.shape[0]
     lw = _Lowerer(flags, S)
     binds = element_bindings(flat, parameters)
+    coord_cols = set(parse_parameters(parameters)[0].values())
     per, pre = fractures(len(flat), where)
     for idx, elem in enumerate(flat):
         if pre[idx]:
             lw.new_segment()
         prm = {name: Val(seed_values[:, col].copy(), False) for name, col in binds[idx].items()}
-        lower_element(lw, elem, idx, prm, per[idx], binds[idx], seed_values)
+        lower_element(lw, elem, idx, prm, per[idx], binds[idx], seed_values, coord_cols)
     if flags & FMA:
         lw.segments = [_merge_drifts(seg) for seg in lw.segments]
     if dump_end is None:

@@ -120,6 +120,15 @@ class _Compiled:
         return self._dprog
 
 
+def _no_turn(prog, what):
+    """The reference's closed-orbit and optics kernels declare no ``turn``
+    (ufo/co.py:146-250, ufo/optics.py:87-154): element text that reads it fails
+    their OpenCL build, and fails here the same way."""
+    if C.reads_turn(prog):
+        raise RuntimeError(f'an aperture window or element strength reads `turn`, which the '
+                           f'{what} kernel does not define')
+
+
 def _coords_from_pool(pool, parameters, flags, dp):
     n = pool.shape[0]
     coords = np.zeros((n, 6))
@@ -306,6 +315,7 @@ class ClosedOrbit:
         self._line = _snapshot(line)
         # dp = 0, oodppo = 1, z = 0 are forced by the reference (ufo/co.py:182-184)
         self._c = _Compiled(self._line, flags & ~FIVED, parameters, [])
+        _no_turn(self._c.prog, 'closed-orbit')
         self.src = self._c.prog.describe()
 
     def run(self, threads=1):
@@ -360,6 +370,7 @@ class Optics:
             raise Exception("No valid observation points found in 'where'")
         self._line = _snapshot(line)
         self._c = _Compiled(self._line, flags, parameters, where, count=self.count)
+        _no_turn(self._c.prog, 'optics')
         self.track = np.zeros([3, self.count, 6], dtype=_ufloat(flags))
         self.src = self._c.prog.describe()
         self.ax0 = self.bx0 = self.dx0 = self.dpx0 = 0.
