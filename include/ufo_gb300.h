@@ -62,7 +62,8 @@ void ufo_ctx_destroy(ufo_ctx *ctx);
 int ufo_prog_create(ufo_ctx *ctx, const int32_t *ops, int n_ops, const double *table,
                     int64_t stride, int n_seeds, int n_dumps, ufo_prog **out);
 /* Replace the per-seed constants (same stride); new parameter values between
- * runs, the role of the reference's `.parameters` buffer for lattice values. */
+ * runs, the role of the reference's `.parameters` buffer for lattice values.
+ * Every row's aperture and dynamic-kick programs are checked as at creation. */
 int ufo_prog_set_table(ufo_prog *prog, const double *table, int n_seeds);
 void ufo_prog_destroy(ufo_prog *prog);
 

@@ -264,20 +264,25 @@ def test_coordinate_columns_are_not_lattice_values():
 
 @pytest.mark.gpu
 def test_malformed_dynamic_kick_tables_rejected_before_launch():
-    """ufo_prog_create checks every dynamic-kick program on the host: a length
-    past the op's table words or an op without operands is an error, and no
-    kernel runs."""
+    """ufo_prog_create and ufo_prog_set_table check every dynamic-kick program
+    on the host: a length past the op's table words or an op without operands
+    is an error, and no kernel runs."""
     import kickers
     import ufo_gb300 as u
     from ufo_gb300 import capi, cexpr, compiler as C
     line = u.Line('L', [kickers.NLKGate('N', knl=[0., 1e-3]), u.Drift('D', length=1.0)])
     prog = C.compile_line(line, u.KICK, [], [-1])
     ctx = u.context(0)
-    capi.DeviceProgram(ctx, prog)  # well formed
+    good = capi.DeviceProgram(ctx, prog)  # well formed
     # table: [1, PUSH, 0.0, 6, VAR, 7, PUSH, 20, EQ, 0, ...]
     for pos, value in ((0, 99.0), (4, float(cexpr.NEG))):
+        bad = prog.table.copy()
+        bad[0, pos] = value
+        with pytest.raises(RuntimeError, match='dynamic-kick'):
+            good.set_table(bad)  # a replacement table is checked the same way
         keep = prog.table[0, pos]
         prog.table[0, pos] = value
         with pytest.raises(RuntimeError, match='dynamic-kick'):
             capi.DeviceProgram(ctx, prog)
         prog.table[0, pos] = keep
+    good.set_table(prog.table)

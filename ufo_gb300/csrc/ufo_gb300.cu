@@ -20,6 +20,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "../../include/ufo_gb300.h"
 #include "ops.cuh"
@@ -422,6 +423,7 @@ struct ufo_prog {
   int n_seeds;
   int n_dumps;
   bool full;  // needs the full interpreter (thick, wire, exact, ...)
+  std::vector<int32_t> host_ops;  // for validating replacement tables
 };
 
 namespace {
@@ -815,13 +817,23 @@ int ufo_launch_count(ufo_ctx *ctx, int64_t *count) {
   return UFO_OK;
 }
 
+// the op shapes, and every seed row's expression programs
+static int validate_rows(const int32_t *ops, int n_ops, int64_t stride, const double *table,
+                  int n_seeds) {
+  for (int r = 0; r < n_seeds; ++r) {
+    const int rc = validate_ops(ops, n_ops, stride, table + static_cast<int64_t>(r) * stride);
+    if (rc) return rc;
+  }
+  return UFO_OK;
+}
+
 int ufo_prog_create(ufo_ctx *ctx, const int32_t *ops, int n_ops, const double *table,
                     int64_t stride, int n_seeds, int n_dumps, ufo_prog **out) {
   if (!ctx || !ops || !table || !out) return fail(UFO_E_ARG, "null argument");
   *out = nullptr;
   if (n_ops < 0 || stride < 1 || n_seeds < 1 || n_dumps < 0)
     return fail(UFO_E_ARG, "bad program sizes");
-  int rc = validate_ops(ops, n_ops, stride, table);
+  int rc = validate_rows(ops, n_ops, stride, table, n_seeds);
   if (rc) return rc;
   UFO_CUDA(cudaSetDevice(ctx->device));
   ufo_prog *p = new (std::nothrow) ufo_prog;
@@ -833,6 +845,7 @@ int ufo_prog_create(ufo_ctx *ctx, const int32_t *ops, int n_ops, const double *t
   p->n_seeds = n_seeds;
   p->n_dumps = n_dumps;
   p->full = needs_full(ops, n_ops);
+  p->host_ops.assign(ops, ops + static_cast<size_t>(n_ops) * UFO_OP_WORDS);
   p->ops = nullptr;
   p->table = nullptr;
   const size_t ob = sizeof(ufo::Op) * (n_ops > 0 ? n_ops : 1);
@@ -861,6 +874,8 @@ int ufo_prog_create(ufo_ctx *ctx, const int32_t *ops, int n_ops, const double *t
 int ufo_prog_set_table(ufo_prog *prog, const double *table, int n_seeds) {
   if (!prog || !table) return fail(UFO_E_ARG, "null argument");
   if (n_seeds != prog->n_seeds) return fail(UFO_E_ARG, "seed count changed");
+  const int rc = validate_rows(prog->host_ops.data(), prog->n_ops, prog->stride, table, n_seeds);
+  if (rc) return rc;
   UFO_CUDA(cudaSetDevice(prog->ctx->device));
   const size_t tb = sizeof(double) * static_cast<size_t>(prog->stride) * n_seeds;
   UFO_CUDA(cudaMemcpyAsync(prog->table, table, tb, cudaMemcpyHostToDevice, prog->ctx->stream));
