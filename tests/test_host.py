@@ -85,12 +85,27 @@ def test_fractures_follow_reference():
     assert per[0] == [0.5] and per[1] == [0.25] and per[2] == [0.75] and per[3] == []
 
 
-def test_user_method_override_rejected():
-    class NLK(u.Multipole):
+def test_user_method_returning_opencl_rejected():
+    """An override that returns its own OpenCL (not its base class's
+    method() result) cannot run in the data-driven kernels."""
+    class Raw(u.Multipole):
         def method(self, **kw):
             return ['x += 1;']
     with pytest.raises(NotImplementedError):
-        C.compile_line(u.Line('l', [NLK('n', knl=[0, 1])]), 0, [], [-1])
+        C.compile_line(u.Line('l', [Raw('n', knl=[0, 1])]), 0, [], [-1])
+
+
+def test_line_method_lowers_every_element_type():
+    """What the reference's tests/elements.py checks (every element type of
+    elements.mad lowers), in thick and kick modes, and fractures split the
+    program into one segment per interval."""
+    line = H.line_of(H.case('elements_kick'))
+    kinds = {e.kind for e in line.flatten()}
+    assert kinds == {'drift', 'quadrupole', 'sbend', 'sextupole', 'multipole', 'marker'}
+    for flags in (0, u.KICK, u.KICK | u.EXACT, u.LINEAR | u.ACHROMATIC):
+        segs = line.method(flags=flags)
+        assert len(segs) == 1 and len(segs[0]) > 0
+    assert len(line.method(fracture=[1.5, 3.25], flags=u.KICK)) == 3
 
 
 def test_madx_loader():
