@@ -105,7 +105,8 @@ def test_line_method_lowers_every_element_type():
     for flags in (0, u.KICK, u.KICK | u.EXACT, u.LINEAR | u.ACHROMATIC):
         segs = line.method(flags=flags)
         assert len(segs) == 1 and len(segs[0]) > 0
-    assert len(line.method(fracture=[1.5, 3.25], flags=u.KICK)) == 3
+    assert len(line.method(fracture=[1.5, 4.25], flags=u.KICK)) == 3  # bend, sextupole
+    assert len(line.method(fracture=[3.5], flags=u.KICK)) == 1  # a marker drops it (thin)
 
 
 def test_madx_loader():
