@@ -249,12 +249,23 @@ def main(ref):
                  f'{k1} * sin(3.1415 * ((float)turn - {t0}) / {tau}): 0.')
             return super().method(k1=f'({k})', **kwargs)
 
+    class SkewKick(ufo.Multipole):
+        # a sextupole term every third turn and a skew quadrupole that flips
+        # sign after turn 4: higher orders and the skew Horner of a
+        # time-dependent kick
+        def method(self, k2=None, k1s=None, **kwargs):
+            k2, k1s = k2 or self.knl[2], k1s or self.ksl[1]
+            return super().method(k2=f'((turn % 3 == 0) ? {k2} : 0.)',
+                                  k1s=f'((turn > 4) ? {k1s} : -{k1s})', **kwargs)
+
     rng = np.random.default_rng(7)
     betax, ex0 = 11.26, 4.3e-9
     for name, kicker, turns, n, params, extra in (
             ('nlk_gate', NLKGate('NLK', knl=[0., 5e-2]), 40, 32, ['x', 'px'], {}),
             ('nlk_pulse', NLKPulse('NLK', knl=[0., 5e-2], tau=1.5), 15, 28,
-             ['x', 'px', ('NLK', 't0')], {'tau': 1.5})):
+             ['x', 'px', ('NLK', 't0')], {'tau': 1.5}),
+            ('skew_kick', SkewKick('SK', knl=[0., 0., 40.0], ksl=[0., 2e-2]), 12, 16,
+             ['x', 'px'], {})):
         ring = lat('alba.mad')
         ring.insert(0, kicker)
         fl = ufo.FIVED | ufo.KICK | ufo.DOUBLE_PRECISION

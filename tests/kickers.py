@@ -29,3 +29,13 @@ class NLKPulse(ufo.Multipole):
         k = (f'((turn >= {t0}) && (turn < {t0} + {tau}) )? '
              f'{k1} * sin(3.1415 * ((float)turn - {t0}) / {tau}): 0.')
         return super().method(k1=f'({k})', **kwargs)
+
+
+class SkewKick(ufo.Multipole):
+    """A sextupole term every third turn and a skew quadrupole that flips sign
+    after turn 4 (orders above 2 and the skew part of a time-dependent kick)."""
+
+    def method(self, k2=None, k1s=None, **kwargs):
+        k2, k1s = k2 or self.knl[2], k1s or self.ksl[1]
+        return super().method(k2=f'((turn % 3 == 0) ? {k2} : 0.)',
+                              k1s=f'((turn > 4) ? {k1s} : -{k1s})', **kwargs)
