@@ -96,7 +96,7 @@ def _div(a, b):
 class Prepared:
     """Per-seed element records of a line, ready for oracle_track."""
 
-    def __init__(self, line, flags, parameters, where, seed_values):
+    def __init__(self, line, flags, parameters, where, seed_values, dp=0.0):
         from ufo_gb300 import compiler, aperture
         flat = line.flatten() if hasattr(line, 'flatten') else list(line)
         parameters = list(parameters)
@@ -125,6 +125,12 @@ class Prepared:
                 for opc, v in code:
                     ap += [float(opc), float(v)]
         achro = bool(flags & ACHROMATIC)
+        # FIVED pastes dp as a literal (ufo/track.py:99-101), so oodppo is a
+        # compile-time constant and the C compiler folds what it feeds: the
+        # thick maps' and fringe edges' transcendentals, as in ACHROMATIC mode
+        fived = bool(flags & FIVED)
+        o_lit = float(np.float64(1.0) / (np.float64(dp) + np.float64(1.0)))
+        fold_mode = achro or fived
         for s in range(S):
             for idx, e in enumerate(flat):
                 r = elems[s * n + idx]
@@ -210,8 +216,10 @@ class Prepared:
                         c, sn, t = _fold('cos', ev, elit), _fold('sin', ev, elit), \
                             _fold('tan', ev, elit)
                         tpsi = 0.0
-                        if achro:
+                        if fold_mode:
                             curv = _div(A, L)
+                            if not achro:  # angle / (L) * oodppo
+                                curv = float(np.float64(curv) * np.float64(o_lit))
                             with np.errstate(all='ignore'):
                                 psi = float(np.float64(ev) - np.float64(2 * curv) *
                                             np.float64(fringe) / np.float64(c) *
@@ -219,16 +227,21 @@ class Prepared:
                             tpsi = _fold('tan', psi, elit and lit_edge)
                         fl[4 * j:4 * j + 4] = [c, sn, t, tpsi]
                 thick = not (flags & KICK) and e.kind in ('quadrupole', 'sbend', 'rbend')
-                if thick and achro:
+                if e.kind in ('sbend', 'rbend') and fold_mode:
+                    r['fold_achro'] = 1  # the edges' tan(psi) come from the fold slots
+                if thick and fold_mode:
                     r['fold_achro'] = 1
                     L = float(r['length'])
                     k1 = float(r['k1'])
                     tl = lit.get('length', True) and lit.get('k1', True)
+                    o = 1.0 if achro else o_lit
                     for f in pieces:
                         with np.errstate(all='ignore'):
                             Lf = float(np.float64(L) * np.float64(f))
                         if e.kind == 'quadrupole':
-                            k2 = _sqrt(abs(k1))
+                            with np.errstate(all='ignore'):
+                                k2 = _sqrt(abs(k1) if achro else
+                                           abs(float(np.float64(k1) * np.float64(o))))
                             k2l = Lf * k2
                             fl += [_fold('cos', k2l, tl), _fold('sin', k2l, tl),
                                    _fold('cosh', k2l, tl), _fold('sinh', k2l, tl)]
@@ -238,12 +251,19 @@ class Prepared:
                             Af = float(np.float64(A) * np.float64(f))
                             curv = _div(Af, Lf)
                             kv = k1
+                            if not achro:  # curvature and k carry oodppo
+                                with np.errstate(all='ignore'):
+                                    curv = float(np.float64(curv) * np.float64(o))
+                                    kv = float(np.float64(k1) * np.float64(o))
                             k2 = _sqrt(abs(kv))
                             k2l = Lf * k2
                             v = [_fold('cos', k2l, tlb), _fold('sin', k2l, tlb),
                                  _fold('cosh', k2l, tlb), _fold('sinh', k2l, tlb)]
                             with np.errstate(all='ignore'):
-                                kx = float(np.float64(kv) + np.float64(curv) * np.float64(curv))
+                                cc = np.float64(curv) * np.float64(curv)
+                                if not achro:  # k += curvature * curvature / oodppo
+                                    cc = cc / np.float64(o)
+                                kx = float(np.float64(kv) + cc)
                             k2 = _sqrt(abs(kx))
                             k2l = Lf * k2
                             v += [_fold('cos', k2l, tlb), _fold('sin', k2l, tlb),
@@ -316,7 +336,7 @@ def track(line, flags, coords, turns, parameters=(), where=(-1,), seed=None, see
     """Run the oracle.  coords: [n, 6].  Returns dict with tracks [n, count*turns, 6]
     (or None), lost [n] uint32 and final [n, 6]."""
     where = list(where)
-    prep = Prepared(line, flags, parameters, where, seed_values)
+    prep = Prepared(line, flags, parameters, where, seed_values, dp=dp)
     coords = np.ascontiguousarray(coords, dtype=np.float64)
     n = coords.shape[0]
     count = len(where) if count is None else count

@@ -49,7 +49,8 @@ typedef struct {
     int32_t nknl, nksl, ndkn, ndks, mp_off;   /* knl | ksl | dkn | dks */
     int32_t nfrac, frac_off, pre_dump;        /* fracture fractions, dump before */
     int32_t ap_off, ap_len;                   /* (opcode, value) pairs */
-    int32_t fold_off, fold_achro;             /* folded constants offset */
+    int32_t fold_off, fold_achro;             /* folded constants offset; set when oodppo
+                                                 is a compile-time constant */
     double length, angle, k1, e1, e2, hgap, fint, dx, dy, k2, k2s, k3, k3s, wx, wy, wk;
 } oelem;
 
@@ -139,11 +140,13 @@ static void teapot_(state *s, int flags, double L, double f, int N, const double
 
 /* edge: curvature = angle/(L) (* oodppo); psi = e - 2*curv*fringe/cos(e)*(1+sin^2 e)
  * fold[0..3] = cos(e), sin(e), tan(e), tan(psi) (the last only if achromatic) */
+/* fold[3] holds tan(psi) when oodppo is a compile-time constant (ACHROMATIC,
+ * or FIVED's literal dp): `folded` */
 static void edge_(state *s, int flags, double L, double angle, double e, double fringe,
-                  const double *fold) {
+                  const double *fold, int folded) {
     double curvature = (flags & F_ACHRO) ? angle / L : angle / L * s->oodppo;
     double tpsi;
-    if (flags & F_ACHRO) {
+    if ((flags & F_ACHRO) || folded) {
         tpsi = fold[3];
     } else {
         double psi = e - 2 * curvature * fringe / fold[0] * (1. + fold[1] * fold[1]);
@@ -350,7 +353,8 @@ static void one_turn_(state *s, int flags, const oelem *el, int n, const double 
                     align_(s, q->dx, q->dy);
                     if (q->type == T_SBEND || q->type == T_RBEND) {
                         double e1 = q->type == T_RBEND ? q->e1 + (q->angle * 0.5) : q->e1;
-                        edge_(s, flags, q->length, q->angle, e1, (q->hgap * q->fint), fl);
+                        edge_(s, flags, q->length, q->angle, e1, (q->hgap * q->fint), fl,
+                              q->fold_achro);
                     }
                 }
                 /* multipole lists: knl = pad(dkn, order), knl[order-1] += main */
@@ -390,7 +394,8 @@ static void one_turn_(state *s, int flags, const oelem *el, int n, const double 
                 if (i == np - 1 && q->type != T_DRIFT) {
                     if (q->type == T_SBEND || q->type == T_RBEND) {
                         double e2 = q->type == T_RBEND ? q->e2 + (q->angle * 0.5) : q->e2;
-                        edge_(s, flags, q->length, q->angle, e2, (q->hgap * q->fint), fl + 4);
+                        edge_(s, flags, q->length, q->angle, e2, (q->hgap * q->fint), fl + 4,
+                              q->fold_achro);
                     }
                     align_(s, -(q->dx), -(q->dy));
                 }

@@ -98,6 +98,11 @@ def main(ref):
     track_case('alba_thick', lat('alba.mad'), 0, 10, 8, six, [-1])
     track_case('alba_kick', lat('alba.mad'), ufo.KICK, 10, 8, six, [-1])
     track_case('alba_kick_exact', lat('alba.mad'), ufo.KICK | ufo.EXACT, 10, 8, six, [-1])
+    # FIVED pastes dp as a literal: the C compiler folds the thick maps' and
+    # fringe edges' transcendentals (the HOWTO's own mode)
+    four = ['x', 'px', 'y', 'py']
+    track_case('alba_fived_thick', lat('alba.mad'), ufo.FIVED, 10, 8, four, [-1])
+    track_case('alba_fived_thick_dp', lat('alba.mad'), ufo.FIVED, 10, 8, four, [-1], dp=1e-3)
     track_case('alba_linear_achro', lat('alba.mad'), ufo.LINEAR | ufo.ACHROMATIC, 3, 4, six, [-1])
     track_case('alba_achro_thick', lat('alba.mad'), ufo.ACHROMATIC, 3, 4, six, [-1])
     track_case('elements_kick', lat('elements.mad', 'TEST'), ufo.KICK, 30, 8, six, [-1, 1.5])
