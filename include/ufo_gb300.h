@@ -29,7 +29,6 @@ extern "C" {
 #define UFO_E_ARG (-1)       /* invalid argument (sizes, NULL, opcode table) */
 #define UFO_E_CUDA (-2)      /* CUDA runtime error */
 #define UFO_E_NOMEM (-3)     /* device allocation failed */
-#define UFO_E_TIMEOUT (-4)   /* a bounded device wait gave up */
 
 /* track modes: loss test at the end of each turn */
 #define UFO_MODE_TRACK 0     /* isnan(x)                        ufo/track.py:107-108 */
@@ -116,7 +115,18 @@ int ufo_track_device(ufo_ctx *ctx, const ufo_prog *prog, const double *d_coords,
  * shares that array: calls that overlap on the GPU race (serialise them on one
  * stream); each call clears the counter it needs.  The first call on a device
  * sets up that device (resolves the array's address, uploads constant tables);
- * make that first call before any stream capture.
+ * make that first call before any stream capture.  That set-up is not redone:
+ * cudaDeviceReset after the first call is not supported.
+ * `ops` is copied with cudaMemcpyAsync on `stream`: from pageable memory the
+ * call returns after the copy has taken it; from pinned (page-locked) memory
+ * the copy runs later, so keep `ops` unchanged until the stream has passed the
+ * call.  Checks: op shapes, constant offsets against `stride` and observation
+ * indices against `n_dumps` (UFO_E_ARG before any GPU work).  The constants are
+ * on the device, so the aperture and dynamic-kick expression programs inside
+ * `d_table` are NOT checked as ufo_prog_create checks them; pass tables made
+ * by the lattice compiler (ufo_gb300/compiler.py).  A malformed program there
+ * stays in bounds (the kernels bound their expression stacks) but gives a NaN
+ * coefficient or a wrong loss test instead of an error.
  */
 int ufo_track_noalloc(const int32_t *ops, int n_ops, const double *d_table, int64_t stride,
                       int n_seeds, int n_dumps, const double *d_coords, const int32_t *d_seed,

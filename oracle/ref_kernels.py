@@ -24,6 +24,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, '_ref')
 CFLAGS = ['-O2', '-std=gnu11', '-fPIC', '-shared', '-ffp-contract=off', '-fno-fast-math',
           '-fopenmp', '-w']
+# the reference's own default build options, -cl-fast-relaxed-math -cl-mad-enable
+# (ufo/__init__.py:22), in gcc's terms: contraction and fast math allowed.  A
+# speed figure only; parity is held against the strict build above.
+CFLAGS_FAST = ['-O3', '-std=gnu11', '-fPIC', '-shared', '-ffast-math', '-ffp-contract=fast',
+               '-fopenmp', '-w']
 
 # benchmark samples: (name, workload, particles, turns)
 SAMPLES = [('c2_track', 'c2', 16384, 100), ('c1_track', 'c1', 8192, 200)]
@@ -52,35 +57,52 @@ def generate(ref_path):
                        'elements': len(ring.flatten()), 'count': tr.count}, f)
 
 
+def _so(name, fast):
+    return os.path.join(OUT, f'{name}_fast.so' if fast else f'{name}.so')
+
+
 def build_all(quiet=False):
+    """Compile every generated kernel twice: strict IEEE (the parity build,
+    ``<name>.so``) and under the reference's default fast-math options
+    (``<name>_fast.so``)."""
     if not os.path.isdir(OUT):
         raise FileNotFoundError('no generated reference kernels (oracle/_ref)')
-    built = []
+    jobs = []
     for f in sorted(os.listdir(OUT)):
         if not f.endswith('.c'):
             continue
         src = os.path.join(OUT, f)
-        so = src[:-2] + '.so'
-        if os.path.exists(so) and os.path.getmtime(so) >= os.path.getmtime(src):
-            built.append(so)
-            continue
-        tmp = so + f'.{os.getpid()}.tmp'
-        subprocess.run(['gcc', *CFLAGS, '-o', tmp, src, '-lm'], check=True)
-        os.replace(tmp, so)
-        built.append(so)
+        for fast in (False, True):
+            so = _so(f[:-2], fast)
+            if os.path.exists(so) and os.path.getmtime(so) >= os.path.getmtime(src):
+                continue
+            tmp = so + f'.{os.getpid()}.tmp'
+            cmd = ['gcc', *(CFLAGS_FAST if fast else CFLAGS), '-o', tmp, src, '-lm']
+            jobs.append((subprocess.Popen(cmd), tmp, so))
+    failed = []
+    for proc, tmp, so in jobs:
+        if proc.wait() == 0:
+            os.replace(tmp, so)
+        else:
+            failed.append(so)
+    if failed:
+        raise RuntimeError(f'gcc failed for {failed}')
+    built = sorted(os.path.join(OUT, f) for f in os.listdir(OUT) if f.endswith('.so'))
     if not quiet:
         print('\n'.join(built))
     return built
 
 
 class RefKernel:
-    """One generated reference kernel: ``run(pool, threads)`` -> tracks."""
+    """One generated reference kernel: ``run(pool, threads)`` -> tracks.
+    ``fast``: the build under the reference's default fast-math options."""
 
-    def __init__(self, name):
+    def __init__(self, name, fast=False):
         self.name = name
+        self.fast = fast
         with open(os.path.join(OUT, f'{name}.json')) as f:
             self.meta = json.load(f)
-        so = os.path.join(OUT, f'{name}.so')
+        so = _so(name, fast)
         if not os.path.exists(so):
             build_all(quiet=True)
         self.lib = ctypes.CDLL(so)

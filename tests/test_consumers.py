@@ -44,6 +44,35 @@ def test_consumers_match_reference_on_its_optics(name):
     assert np.allclose(ch, H.arr(name, 'out/chroma'), rtol=1e-14, atol=0)
 
 
+@pytest.mark.parametrize('name', ['alba_optics_where', 'alba_chroma_fp64', 'alba_radiation_fp64',
+                                  'alba_optics_propagate'])
+def test_twiss_from_reference_unit_tracks(name):
+    """The host Twiss (ufo_gb300/twiss.py) applied to the reference's own
+    unit-particle tracks gives the reference's Twiss functions, tunes and
+    dispersion.  Tolerance: 1e-15 of each array's scale (a few ulps); the
+    propagated alphas of the non-periodic case start from alpha0 ~ 1e-14, so
+    they are compared in absolute terms (1e-15)."""
+    from ufo_gb300 import drivers
+    c = H.case(name)
+    tr = H.arr(name, 'out/track')
+    n = tr.shape[1]
+    o = types.SimpleNamespace(track=tr, periodic=c.get('periodic', True))
+    for k in ('ax', 'ay', 'bx', 'by', 'dx', 'dy', 'dpx', 'dpy', 'mux', 'muy'):
+        setattr(o, k, np.empty(n))
+    o.ax0 = o.bx0 = o.dx0 = o.dpx0 = o.ay0 = o.by0 = o.dy0 = o.dpy0 = 0.
+    for k, v in c.get('attrs', {}).items():
+        setattr(o, k, v)
+    drivers.twiss(o)
+    keys = ['bx', 'by', 'ax', 'ay', 'dx', 'dpx', 'mux', 'muy'] + (['qx', 'qy'] if o.periodic
+                                                                 else [])
+    for k in keys:
+        ref = np.asarray(H.arr(name, f'out/{k}'), dtype=np.float64)
+        got = np.asarray(getattr(o, k), dtype=np.float64)
+        scale = np.max(np.abs(ref))
+        tol = 1e-15 if (k in ('ax', 'ay') and not o.periodic) else 1e-15 * scale + 1e-300
+        assert np.max(np.abs(got - ref)) <= max(tol, 4e-16 * scale), (k, got, ref)
+
+
 def test_reference_consumers_against_madx():
     """What the reference's own tests pin (tests/radiation.py:5-12,
     tests/chroma.py:8-9): I2 is geometry and matches MAD-X; I5 lies within

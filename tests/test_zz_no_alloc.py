@@ -75,3 +75,21 @@ def test_noalloc_rejects_oversized_table_before_touching_the_gpu():
                                0, 0, 1, None, None, None, None)
     assert rc == -1
     assert b'maximum of 8192' in lib.ufo_last_error()
+
+
+@pytest.mark.parametrize('index', [-1, 1])
+def test_noalloc_rejects_observation_index_outside_dumps_before_touching_the_gpu(index):
+    """An observation op writes slot (turn / every) * n_dumps + index of each
+    particle's track rows; an index outside [0, n_dumps) would write into
+    another particle's rows (or before the buffer), so it is refused on the
+    host, before any GPU work."""
+    from ufo_gb300 import capi
+    lib = capi.load()
+    ops = np.zeros((2, 8), dtype=np.int32)
+    ops[0] = [10, 0, 0, 0, 0, 0, 0, 0]       # OP_OBSERVE, index 0: valid
+    ops[1] = [10, 0, 0, index, 0, 0, 0, 0]   # OP_OBSERVE, index outside [0, 1)
+    table = ctypes.c_void_p(1)  # never dereferenced: the op check comes first
+    rc = lib.ufo_track_noalloc(capi.ptr(ops), 2, table, 1, 1, 1, None, None, None, 0, 1, 0,
+                               0, 0, 1, None, None, None, None)
+    assert rc == -1
+    assert b'observation index' in lib.ufo_last_error()

@@ -38,7 +38,7 @@ from . import crmath
 from . import elements as E
 from .flags import LINEAR, FIVED, EXACT, KICK, ACHROMATIC, YOSHIDA, FMA
 
-# ---- opcodes (shared with csrc/ufo_kernels.cuh and oracle) ----
+# ---- opcodes (the same numbering as csrc/ops.cuh) ----
 OP_NOP, OP_DRIFT, OP_KICK, OP_TEAPOT, OP_ALIGN, OP_EDGE, OP_THICKQ, OP_THICKB, OP_WIRE, \
     OP_APERTURE, OP_OBSERVE, OP_DYNKICK = range(12)
 OP_NAMES = ['nop', 'drift', 'kick', 'teapot', 'align', 'edge', 'thickq', 'thickb', 'wire',

@@ -19,6 +19,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -75,7 +76,7 @@ UFO_DEV void observe(const State &s, const TrackArgs &a, int64_t p, int k) {
   if (!a.tracks) return;
   if ((s.turn + 1) % a.every) return;
   const int64_t slot = static_cast<int64_t>((s.turn + 1) / a.every - 1) * a.n_dumps + k;
-  if (slot >= a.slots) return;
+  if (slot < 0 || slot >= a.slots) return;
   double *t = a.tracks + (p * a.slots + slot) * 6;
   t[0] = s.x; t[1] = s.px; t[2] = s.y; t[3] = s.py;
   if (!(a.flags & UFO_TRACK_FIVED)) { t[4] = s.z; t[5] = s.dp; }
@@ -447,10 +448,15 @@ int cuda_fail(cudaError_t e, const char *what) {
     if (e_ != cudaSuccess) return cuda_fail(e_, #call); \
   } while (0)
 
+// per-device set-up state; host threads making their first call on a device
+// at the same time serialise on this mutex
+std::mutex g_setup_mutex;
 bool g_const_ready[64] = {};
 
+// Upload the constant tables to the current device, once per device.
 int ensure_constants(int device) {
   if (device < 0 || device >= 64) return fail(UFO_E_ARG, "device %d out of range", device);
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
   if (g_const_ready[device]) return UFO_OK;
   double r[33];
   r[0] = 0.0;
@@ -587,11 +593,17 @@ bool needs_full(const int32_t *ops, int n_ops) {
   return false;
 }
 
-int validate_ops(const int32_t *ops, int n_ops, int64_t stride, const double *table) {
+// `table` may be NULL (constants on the device): the expression programs of
+// apertures and dynamic kicks are then not checked.
+int validate_ops(const int32_t *ops, int n_ops, int64_t stride, int n_dumps,
+                 const double *table) {
   for (int i = 0; i < n_ops; ++i) {
     const int32_t *w = ops + i * UFO_OP_WORDS;
     if (w[0] < ufo::OP_NOP || w[0] > ufo::OP_DYNKICK)
       return fail(UFO_E_ARG, "op %d: unknown kind %d", i, w[0]);
+    // an observation point writes slot (turn / every) * n_dumps + index
+    if (w[0] == ufo::OP_OBSERVE && (w[3] < 0 || w[3] >= n_dumps))
+      return fail(UFO_E_ARG, "op %d: observation index %d outside [0, %d)", i, w[3], n_dumps);
     const int64_t nc = op_consts(w);
     if (nc < 0) return fail(UFO_E_ARG, "op %d (kind %d): invalid shape", i, w[0]);
     if (w[2] < 0 || w[2] + nc > stride)
@@ -818,10 +830,11 @@ int ufo_launch_count(ufo_ctx *ctx, int64_t *count) {
 }
 
 // the op shapes, and every seed row's expression programs
-static int validate_rows(const int32_t *ops, int n_ops, int64_t stride, const double *table,
-                  int n_seeds) {
+static int validate_rows(const int32_t *ops, int n_ops, int64_t stride, int n_dumps,
+                         const double *table, int n_seeds) {
   for (int r = 0; r < n_seeds; ++r) {
-    const int rc = validate_ops(ops, n_ops, stride, table + static_cast<int64_t>(r) * stride);
+    const int rc =
+        validate_ops(ops, n_ops, stride, n_dumps, table + static_cast<int64_t>(r) * stride);
     if (rc) return rc;
   }
   return UFO_OK;
@@ -833,7 +846,7 @@ int ufo_prog_create(ufo_ctx *ctx, const int32_t *ops, int n_ops, const double *t
   *out = nullptr;
   if (n_ops < 0 || stride < 1 || n_seeds < 1 || n_dumps < 0)
     return fail(UFO_E_ARG, "bad program sizes");
-  int rc = validate_rows(ops, n_ops, stride, table, n_seeds);
+  int rc = validate_rows(ops, n_ops, stride, n_dumps, table, n_seeds);
   if (rc) return rc;
   UFO_CUDA(cudaSetDevice(ctx->device));
   ufo_prog *p = new (std::nothrow) ufo_prog;
@@ -874,7 +887,8 @@ int ufo_prog_create(ufo_ctx *ctx, const int32_t *ops, int n_ops, const double *t
 int ufo_prog_set_table(ufo_prog *prog, const double *table, int n_seeds) {
   if (!prog || !table) return fail(UFO_E_ARG, "null argument");
   if (n_seeds != prog->n_seeds) return fail(UFO_E_ARG, "seed count changed");
-  const int rc = validate_rows(prog->host_ops.data(), prog->n_ops, prog->stride, table, n_seeds);
+  const int rc = validate_rows(prog->host_ops.data(), prog->n_ops, prog->stride, prog->n_dumps,
+                               table, n_seeds);
   if (rc) return rc;
   UFO_CUDA(cudaSetDevice(prog->ctx->device));
   const size_t tb = sizeof(double) * static_cast<size_t>(prog->stride) * n_seeds;
@@ -1002,10 +1016,11 @@ NoallocDevice g_noalloc_dev[64];
 // constant tables.  Runs on a device's first call.
 int noalloc_setup(int device) {
   if (device < 0 || device >= 64) return fail(UFO_E_ARG, "device %d out of range", device);
-  NoallocDevice &d = g_noalloc_dev[device];
-  if (d.ready) return UFO_OK;
   int rc = ensure_constants(device);
   if (rc) return rc;
+  std::lock_guard<std::mutex> lock(g_setup_mutex);
+  NoallocDevice &d = g_noalloc_dev[device];
+  if (d.ready) return UFO_OK;
   void *ptr = nullptr;
   cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
   if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
@@ -1037,7 +1052,9 @@ extern "C" int ufo_track_noalloc(const int32_t *ops, int n_ops, const double *d_
   if (mode != UFO_MODE_TRACK && mode != UFO_MODE_SA) return fail(UFO_E_ARG, "bad mode %d", mode);
   if (slots < 0 || every < 1) return fail(UFO_E_ARG, "bad observation slots or stride");
   if (n > 0 && !d_coords) return fail(UFO_E_ARG, "null coordinates");
-  int rc = validate_ops(ops, n_ops, stride, nullptr);
+  // the constants are on the device: op shapes and observation indices are
+  // checked here, expression programs are not (see the header)
+  int rc = validate_ops(ops, n_ops, stride, n_dumps, nullptr);
   if (rc) return rc;
   int device = 0;
   UFO_CUDA(cudaGetDevice(&device));

@@ -19,6 +19,7 @@ import numpy as np
 
 from . import capi
 from . import compiler as C
+from . import twiss as _twiss
 from .flags import FIVED, DOUBLE_PRECISION, LINEAR, ACHROMATIC, FMA, KICK
 
 COORDS = ('x', 'px', 'y', 'py', 'z', 'dp')
@@ -319,7 +320,7 @@ class ClosedOrbit:
         self.src = self._c.prog.describe()
 
     def run(self, threads=1):
-        from . import tangent
+        from . import newton_fd
         pool = np.asarray(self.parameters, dtype=np.float64)
         seed_values, seed = self._c.seeds(pool)
         dprog = self._c.device(self.ctx, seed_values)
@@ -336,7 +337,7 @@ class ClosedOrbit:
                 capi.ptr(orbits)))
             self.residual = None
         else:
-            orbits, self.residual = tangent.closed_orbit(self.ctx, dprog, guess, seed=seed,
+            orbits, self.residual = newton_fd.closed_orbit(self.ctx, dprog, guess, seed=seed,
                                                          fma=bool(self.flags & FMA),
                                                          max_iter=self.iterations)
         self.orbits = orbits.astype(self.orbits.dtype, copy=False)
@@ -396,98 +397,13 @@ class Optics:
 
 
 def twiss(o):
-    """Host Twiss/tune/dispersion from the unit tracks, the formulas of
-    ufo/optics.py:156-238."""
-    tr = np.asarray(o.track, dtype=np.float64)
-    if o.periodic:
-        re, im, dp = tr[0][-1], tr[1][-1], tr[2][-1]
-        cos_nu = (re[0] + im[1]) * 0.5
-        if np.absolute(cos_nu) > 1.:
-            o.ax0 = o.bx0 = o.qx = np.nan
-            return
-        o.bx0 = np.absolute(im[0] / np.sin(np.arccos(cos_nu)))
-        sin_nu = im[0] / o.bx0
-        nu = np.arctan2(sin_nu, cos_nu)
-        if nu < 0.:
-            nu += 2. * np.pi
-        o.ax0 = (re[0] - im[1]) / (2. * np.sin(nu))
-        o.qx = nu / (2. * np.pi)
-        k = 2. - re[0] - im[1]
-        o.dx0 = ((1. - im[1]) * dp[0] + im[0] * dp[1]) / k
-        o.dpx0 = ((1. - re[0]) * dp[1] + re[1] * dp[0]) / k
-        cos_nu = (re[2] + im[3]) * 0.5
-        if np.absolute(cos_nu) > 1.:
-            o.ay0 = o.by0 = o.qy = np.nan
-            return
-        o.by0 = np.absolute(im[2] / np.sin(np.arccos(cos_nu)))
-        sin_nu = im[2] / o.by0
-        nu = np.arctan2(sin_nu, cos_nu)
-        if nu < 0.:
-            nu += 2. * np.pi
-        o.ay0 = (re[2] - im[3]) / (2. * np.sin(nu))
-        o.qy = nu / (2. * np.pi)
-    for idx, (re, im, dp) in enumerate(zip(tr[0], tr[1], tr[2])):
-        gamma0 = (1. + o.ax0 * o.ax0) / o.bx0
-        o.ax[idx] = -re[0] * re[1] * o.bx0
-        o.ax[idx] += (re[0] * im[1] + im[0] * re[1]) * o.ax0
-        o.ax[idx] += -im[0] * im[1] * gamma0
-        o.bx[idx] = re[0] * re[0] * o.bx0
-        o.bx[idx] += -re[0] * im[0] * o.ax0 * 2.
-        o.bx[idx] += im[0] * im[0] * gamma0
-        o.dx[idx] = re[0] * o.dx0 + im[0] * o.dpx0 + dp[0]
-        o.dpx[idx] = re[1] * o.dx0 + im[1] * o.dpx0 + dp[1]
-        sin_mu = im[0] / np.sqrt(o.bx0 * o.bx[idx])
-        cos_mu = re[0] * np.sqrt(o.bx0 / o.bx[idx]) - o.ax0 * sin_mu
-        o.mux[idx] = np.arctan2(sin_mu, cos_mu)
-        gamma0 = (1. + o.ay0 * o.ay0) / o.by0
-        o.ay[idx] = -re[2] * re[3] * o.by0
-        o.ay[idx] += (re[2] * im[3] + im[2] * re[3]) * o.ay0
-        o.ay[idx] += -im[2] * im[3] * gamma0
-        o.by[idx] = re[2] * re[2] * o.by0
-        o.by[idx] += -re[2] * im[2] * o.ay0 * 2.
-        o.by[idx] += im[2] * im[2] * gamma0
-        o.dy[idx] = re[2] * o.dy0 + im[2] * o.dpy0 + dp[2]
-        o.dpy[idx] = re[3] * o.dy0 + im[3] * o.dpy0 + dp[3]
-        sin_mu = im[2] / np.sqrt(o.by0 * o.by[idx])
-        cos_mu = re[2] * np.sqrt(o.by0 / o.by[idx]) - o.ay0 * sin_mu
-        o.muy[idx] = np.arctan2(sin_mu, cos_mu)
+    """Twiss, tunes and dispersion of an Optics object from its unit tracks
+    (ufo_gb300/twiss.py)."""
+    _twiss.twiss(o)
 
 
 def chromaticity(optics):
-    """Analytic natural + sextupole chromaticity from Twiss at element starts
-    (the formulas of ufo/chroma.py:11-52).  Returns ((dqx0, dqy0), (dqx, dqy))."""
-    dqx0 = dqy0 = dqx = dqy = 0.
-    for (_, element), ax, ay, bx, by, dx, dpx in zip(optics.where, optics.ax, optics.ay,
-                                                     optics.bx, optics.by, optics.dx, optics.dpx):
-        l = getattr(element, 'length', 0.)
-        k = getattr(element, 'k1', 0.)
-        if l != 0 and k != 0:
-            k2 = np.sqrt(np.absolute(k))
-            k2l = l * k2
-            gx = (1. + ax * ax) / bx
-            gy = (1. + ay * ay) / by
-            S = np.sin(2. * k2l) / 4. / k2
-            SH = np.sinh(2. * k2l) / 4. / k2
-            Cc = (np.cos(k2l) ** 2 - 1.) / k2 / k2
-            CH = (np.cosh(k2l) ** 2 - 1.) / k2 / k2
-            if k > 0:
-                dqx0 -= (bx * (l / 2. + S) + ax * Cc + gx * (l / 2. - S) / k2 / k2) * k
-                dqy0 += (by * (l / 2. + SH) - ay * CH - gy * (l / 2. - SH) / k2 / k2) * k
-            else:
-                dqy0 += (by * (l / 2. + S) + ay * Cc + gy * (l / 2. - S) / k2 / k2) * k
-                dqx0 -= (bx * (l / 2. + SH) - ax * CH - gx * (l / 2. - SH) / k2 / k2) * k
-        k = getattr(element, 'k2', 0.)
-        if l != 0 and k != 0:
-            gx = (1. + ax * ax) / bx
-            gy = (1. + ay * ay) / by
-            dqx += (dx * (bx + (gx * l / 3. - ax) * l) + dpx * l *
-                    (bx / 2. - l * (2. * ax / 3. + gx * l / 4.))) * l * k
-            dqy -= (dx * (by + (gy * l / 3. - ay) * l) + dpx * l *
-                    (by / 2. - l * (2. * ay / 3. + gy * l / 4.))) * l * k
-    dqx0 /= 4. * np.pi
-    dqy0 /= 4. * np.pi
-    dqx /= 4. * np.pi
-    dqy /= 4. * np.pi
-    dqx += dqx0
-    dqy += dqy0
-    return (dqx0, dqy0), (dqx, dqy)
+    """Analytic natural and total linear chromaticity from Twiss at the
+    elements' entrances (the reference's ufo/chroma.py:11-52; computed in
+    ufo_gb300/twiss.py).  Returns ((dqx0, dqy0), (dqx, dqy))."""
+    return _twiss.chromaticity(optics)

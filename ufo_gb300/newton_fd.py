@@ -1,4 +1,4 @@
-"""Closed orbit by Newton iteration on the one-turn map.
+"""Closed orbit by Newton iteration with a finite-difference Jacobian.
 
 F(z) = z is solved for z = (x, px, y, py) at dp = 0 (the reference's
 ClosedOrbit forces dp = 0, oodppo = 1, z = 0: ufo/co.py:182-184).  Each Newton
@@ -6,7 +6,8 @@ step evaluates F at the iterate and at 8 central-difference points for every
 orbit in ONE batched launch of the tracking kernel (the reference's
 per-particle-parameter batching idiom), then solves (J - I) dz = z - F(z) on
 the host.  The fixed point itself is exact FP64 tracking; the Jacobian only
-steers the iteration.
+steers the iteration.  (The differentiator, ufo_gb300/diff.py, has a Newton
+iteration on the exact tangent map instead: OpticsModel.)
 """
 import numpy as np
 
