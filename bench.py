@@ -60,8 +60,8 @@ def parse():
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--workload', default='c2', choices=['c2', 'c3', 'c4', 'c5'])
-    ap.add_argument('--seeds', type=int, default=64, help='C4: number of seeds')
-    ap.add_argument('--turn-div', type=int, default=4, help='C4: divide turn counts by this')
+    ap.add_argument('--seeds', type=int, default=512, help='C4: number of seeds')
+    ap.add_argument('--turn-div', type=int, default=1, help='C4: divide turn counts by this')
     ap.add_argument('--c5-seeds', type=int, default=256,
                     help='C5: error seeds in the GPU-filling adjoint batch')
     ap.add_argument('--c5-fd-params', type=int, default=8,
@@ -70,6 +70,14 @@ def parse():
                     help='print the FP64-pipe probe table (latency, occupancy, active lanes)')
     ap.add_argument('--c5-skip-multiturn', action='store_true',
                     help='C5: optics gradients only (for profiling captures)')
+    ap.add_argument('--op-mix', action='store_true',
+                    help='one small launch per element type and mode (for an ncu op-mix capture)')
+    ap.add_argument('--no-c4', action='store_true',
+                    help='default line: skip the C4 batched-seed measurement')
+    ap.add_argument('--no-c5', action='store_true',
+                    help='default line: skip the C5 adjoint measurement')
+    ap.add_argument('--no-c3', action='store_true',
+                    help='default line: skip the C3 dynamic-aperture measurement')
     return ap.parse_args()
 
 
@@ -128,10 +136,12 @@ class Clocks:
                 'samples': len(rows)}
 
 
-def ref_runner():
+def ref_runner(fast=False):
     """The reference's generated C2 kernel (oracle/_ref) when present, else
     the oracle port; bounded sample of 16,384 particles x 100 turns on all
-    host cores.  Returns (run, sample description, kind, particles, turns)."""
+    host cores.  ``fast``: the build under the reference's default fast-math
+    options instead of the strict (parity) build.
+    Returns (run, sample description, kind, particles, turns, threads)."""
     from ufo_gb300 import workloads as W
     threads = len(os.sched_getaffinity(0))
     n, turns = 16384, 100
@@ -140,10 +150,13 @@ def ref_runner():
         from oracle import ref_kernels as R
         if not R.available('c2_track'):
             raise FileNotFoundError('oracle/_ref/c2_track.c')
-        k = R.RefKernel('c2_track')
+        k = R.RefKernel('c2_track', fast=fast)
         kind = 'reference'
-        desc = ('reference-generated OpenCL C of the C2 ring (its Track kernel), gcc -O2 '
-                '-ffp-contract=off, OpenMP team over its atomic work queue')
+        opts = ('gcc -O3 -ffast-math -ffp-contract=fast (the reference\'s default '
+                '-cl-fast-relaxed-math -cl-mad-enable)' if fast else
+                'gcc -O2 -ffp-contract=off (strict IEEE, the parity build)')
+        desc = ('reference-generated OpenCL C of the C2 ring (its Track kernel), ' + opts +
+                ', OpenMP team over its atomic work queue')
         run = lambda: k.run(beam[:, [0, 1, 2, 3, 5]], threads)  # noqa: E731
     except Exception:  # noqa: BLE001
         import ufo_gb300 as u
@@ -156,8 +169,8 @@ def ref_runner():
     return run, f'C2 ring, {n} particles x {turns} turns per run; {desc}', kind, n, turns, threads
 
 
-def cpu_baseline(ring_elems, runs=2):
-    run, desc, kind, n, turns, threads = ref_runner()
+def cpu_baseline(ring_elems, runs=2, fast=False):
+    run, desc, kind, n, turns, threads = ref_runner(fast)
     run()  # first touch
     best = min(_timed(run) for _ in range(runs))
     return {'value': n * ring_elems * turns / best, 'unit': 'particle*element*turns/s',
@@ -177,7 +190,9 @@ def bench_reference(args):
     from ufo_gb300 import workloads as W
     import ufo_gb300 as u
     ring_elems = len(W.c2_ring(u).flatten())
-    run, desc, kind, n, turns, threads = ref_runner()
+    # the reference's own default build options (fast math, contraction): its
+    # speed as shipped; the strict build is the parity one
+    run, desc, kind, n, turns, threads = ref_runner(fast=True)
     for _ in range(max(0, args.warmup)):
         run()
     sec = sum(_timed(run) for _ in range(args.steps))
@@ -197,14 +212,41 @@ def bench_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def load_traffic(mode):
-    p = os.path.join(HERE, 'profiles', 'track_kernel_c2_traffic.json')
+def load_ncu(mode):
+    """The committed ncu figures of the C2 kernel (profiles/track_kernel_c2_ncu.json):
+    DRAM traffic per launch, FP64-pipe activity, executed flops per particle-turn."""
+    p = os.path.join(HERE, 'profiles', 'track_kernel_c2_ncu.json')
     try:
         with open(p) as f:
-            d = json.load(f)
-        return d.get(mode)
+            return json.load(f).get(mode) or {}
     except (OSError, ValueError):
-        return None
+        return {}
+
+
+def roofline_obj(m, peak, ncu):
+    """The roofline object of a tracking measurement ``m`` (timed_device):
+    FP64-pipe bound.  achieved = executed FP64 flops (the compiler's model of
+    the kernel's instruction mix, FMA = 2, equal to ncu's count on the C2
+    kernel) x particle-turns / mean launch time.  Beside it: the same time
+    against the reference expression's operation count (its arithmetic as
+    written: the strength x oodppo in every slice, divisions by constants),
+    and the committed ncu figures (FP64-pipe activity, DRAM traffic, executed
+    flops measured)."""
+    out = {'bound': 'fp64', 'achieved': m['achieved'], 'peak': peak, 'unit': 'GFLOP/s',
+           'frac': m['achieved'] / peak if peak else None,
+           'traffic': ncu.get('traffic_bytes_per_launch'),
+           'flops_per_particle_turn': m['flops_per_particle_turn'],
+           'flops_basis': 'executed FP64 work (FMA = 2), compiler model of the kernel',
+           'reference_flops_per_particle_turn': m['reference_flops_per_particle_turn'],
+           'frac_reference_expression': m['achieved_reference'] / peak if peak else None,
+           'peak_source': 'measured live: ufo_fp64_peak (DFMA chains, 2 flop each); '
+                          'MEASURED_PEAKS.json has no FP64 figure'}
+    ex = ncu.get('executed_flops_per_particle_turn')
+    if ex and peak:
+        out['frac_executed_ncu'] = ex * m['pt_per_s'] / 1e9 / peak
+    if ncu.get('fp64_pipe_active') is not None:
+        out['fp64_pipe_active_ncu'] = ncu['fp64_pipe_active']
+    return out
 
 
 def bench_ours(args):
@@ -281,12 +323,17 @@ def bench_ours(args):
         lost_np = lost.cpu().numpy()
         # particle-turns tracked by the last launch (a lost particle stops)
         pt = np.where(lost_np < T, lost_np + 1, T).astype(np.float64).sum()
+        # executed FP64 work of the kernel (FMA = 2; the compiler's model of
+        # the instruction mix, equal to ncu's count on the C2 kernel) and the
+        # reference expression's operation count
         fl = prog.flops_fast if mode == 'fma' else prog.flops
-        achieved = fl * pt / (statistics.mean(kern_ms) / 1e3) / 1e9
+        sec = statistics.mean(kern_ms) / 1e3
         return {'value': world * n * n_elem * T * steps / (total_ms / 1e3),
                 'ms_per_step': total_ms / steps, 'kernel_ms': kern_ms,
-                'launches': ctx.launches() - l0, 'achieved': achieved,
-                'flops_per_particle_turn': fl, 'lost': int((lost_np < T).sum())}
+                'launches': ctx.launches() - l0, 'achieved': fl * pt / sec / 1e9,
+                'achieved_reference': prog.flops * pt / sec / 1e9, 'pt_per_s': pt / sec,
+                'flops_per_particle_turn': fl, 'reference_flops_per_particle_turn': prog.flops,
+                'lost': int((lost_np < T).sum())}
 
     clocks = Clocks(local)
     clocks.start()
@@ -320,24 +367,42 @@ def bench_ours(args):
                'h2d_bytes_per_step': n * 6 * 8,
                'd2h_bytes_per_step': n * (6 * 8 + 4 + 6 * 8),
                'api': 'ufo_gb300.Track(...).run() -> ufo_track (host buffers)'}
+    # the other clauses of the metric, measured once on one GPU (rank 0 of a
+    # one-rank run): batched vs one-launch-per-seed (C4), the dynamic-aperture
+    # scan (C3) and the adjoint against finite differences (C5)
+    side = {}
+    if world == 1:
+        if not args.no_c4:
+            side['c4'] = c4_measure(ctx, stream, args.mode, seeds=512, turn_div=1, reps=2,
+                                    warmup=1)
+        if not args.no_c3:
+            side['c3'] = c3_measure(ctx, stream, args.mode)
+        if not args.no_c5:
+            side['c5'] = c5_summary(c5_measure(args, ctx, stream))
     if rank != 0:
         return
-    cb = None if args.no_cpu else cpu_baseline(n_elem)
+    cb = None if args.no_cpu else cpu_baseline(n_elem, fast=True)
+    cbs = None if args.no_cpu else cpu_baseline(n_elem, fast=False)
     line = {
         'metric': 'FP64 particle*element*turns/s', 'value': main['value'],
         'unit': 'particle*element*turns/s', 'n_gpus': world, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': main['ms_per_step'], 'higher_is_better': True,
         'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
-        'config': {'workload': 'C2 light-source ring (1024 elements, teapot 4 slices, 10 mm '
-                               'aperture), 65536 Gaussian particles, 10000 turns',
+        'config': {'workload': f'C2 light-source ring (1024 elements, teapot 4 slices, 10 mm '
+                               f'aperture), {n} Gaussian particles, {args.steps * T} turns '
+                               f'tracked ({args.steps} launches of {T} turns)',
                    'particles_per_gpu': n, 'turns_per_step': T, 'elements': n_elem,
+                   'turns_tracked': args.steps * T,
+                   'deviations_from_spec': [
+                       'ring: 32 identical 12 m cells (384 m, 1024 elements); the specified '
+                       'magnets need 9.22 m per cell, more than 268.8 m / 32',
+                       'integrator: TEAPOT, 4 slices (the reference has no other); the '
+                       'specified 4th-order Yoshida is the yoshida4 object of this line',
+                       'reference arm and cpu_baseline: a sample of 16384 particles x 100 '
+                       'turns per step of the same ring and metric'],
                    'mode': args.mode, 'l2': 'flushed (256 MiB memset) between steps',
                    'parallelism': f'weak: {n} particles per GPU, no collective'},
-        'roofline': {'bound': 'fp64', 'achieved': main['achieved'], 'peak': peak,
-                     'unit': 'GFLOP/s', 'frac': main['achieved'] / peak if peak else None,
-                     'traffic': load_traffic(args.mode),
-                     'flops_per_particle_turn': main['flops_per_particle_turn'],
-                     'peak_source': 'measured live: ufo_fp64_peak (DFMA chains, 2 flop each)'},
+        'roofline': roofline_obj(main, peak, load_ncu(args.mode)),
         'gpu_launches': main['launches'],
         'kernel_ms': main['kernel_ms'],
         'lost_particles': main['lost'],
@@ -361,82 +426,119 @@ def bench_ours(args):
         line['e2e'] = e2e
     if cb:
         line['cpu_baseline'] = {k: cb[k] for k in ('value', 'unit', 'cores', 'kind', 'sample')}
+    if cbs:
+        line['cpu_baseline_strict_ieee'] = {
+            k: cbs[k] for k in ('value', 'unit', 'cores', 'kind', 'sample')}
     if clk:
         line['clocks'] = clk
+    line.update(side)
     print(json.dumps(line), flush=True)
 
 
-def bench_c4(args):
+def c4_measure(ctx, stream, mode, seeds=512, turn_div=1, reps=2, warmup=1, plain=True):
     """Batched error seeds (C4): one autotuned persistent CUDA-graph launch over
-    all seeds vs one launch per seed, identical outputs required."""
+    all seeds, timed ``reps`` times after ``warmup``; then the same seeds with
+    one launch per seed (timed once), whose outputs must be identical.
+    Returns a dict (the C4 object of the bench line)."""
     import torch
     import ufo_gb300 as u
     from ufo_gb300 import workloads as W
-    torch.cuda.set_device(0)
-    ctx = u.context(0)
     parts, turns = W.c4_sizes(512)
-    S = args.seeds
-    parts, turns = parts[:S], np.maximum(1, turns[:S] // args.turn_div)
+    parts, turns = parts[:seeds], np.maximum(1, turns[:seeds] // turn_div)
     ring = W.c1_ring(u)
     params = W.c4_parameters(ring)
-    rows = W.c4_seed_rows(ring, S)
-    flags = u.KICK | (u.FMA if args.mode == 'fma' else 0)
+    rows = W.c4_seed_rows(ring, seeds)
+    flags = u.KICK | (u.FMA if mode == 'fma' else 0)
     b = u.TrackBatch(ring, params, rows, parts, turns, flags=flags, context=ctx)
     b.coords[:] = W.c1_beam(b.n, seed=4)
+    t0 = time.perf_counter()
     tuning = u.autotune(b)
+    tune_s = time.perf_counter() - t0
     pet = b.particle_element_turns()
-    stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
 
-    def timed(fn, reps):
+    def timed(fn, n):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         torch.cuda.synchronize()
         e0.record(stream)
-        for _ in range(reps):
+        for _ in range(n):
             fn()
         e1.record(stream)
         torch.cuda.synchronize()
-        return e0.elapsed_time(e1) / reps
+        return e0.elapsed_time(e1) / n
 
     b.upload()
     b.capture()
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         b.launch(stream=stream.cuda_stream)
-    clocks = Clocks(0)
+    clocks = Clocks(ctx.device)
     clocks.start()
     l0 = ctx.launches()
-    ms_batch = timed(lambda: b.launch(stream=stream.cuda_stream), args.steps)
+    ms_batch = timed(lambda: b.launch(stream=stream.cuda_stream), reps)
     launches = ctx.launches() - l0
     clk = clocks.stop()
     fb, lb = [a.copy() for a in b.download()]
-    b.upload('seed')
-    ms_plain = timed(lambda: b.plain_launches(stream=stream.cuda_stream), 1)
-    fp, lp = b.download()
-    identical = bool(np.array_equal(fb, fp, equal_nan=True) and np.array_equal(lb, lp))
     peak = ctypes_peak(ctx)
     pt_own = np.repeat(b.turns.astype(np.int64), b.particles)
     lb64 = lb.astype(np.int64)
     tracked = float(np.where(lb64 < pt_own, lb64 + 1, pt_own).sum())
-    fl = b.prog.flops_fast if args.mode == 'fma' else b.prog.flops
+    fl = b.prog.flops_fast if mode == 'fma' else b.prog.flops
     achieved = fl * tracked / (ms_batch / 1e3) / 1e9
-    line = {'metric': 'FP64 particle*element*turns/s', 'value': pet / (ms_batch / 1e3),
+    out = {'value': pet / (ms_batch / 1e3), 'unit': 'particle*element*turns/s',
+           'ms_per_launch': ms_batch, 'reps': reps, 'warmup': warmup,
+           'seeds': seeds, 'turn_divisor': turn_div, 'particles': b.n,
+           'particle_element_turns': pet, 'mode': mode, 'tuning': tuning,
+           'autotune_s': tune_s,
+           'workload': f'C4 batched error seeds: {seeds} seeds of the C1 ring (128 elements) with '
+                       f'dx/dy ~ N(0, 50 um) and normal/skew errors of MAD orders 3-6, '
+                       f'particles log-uniform 256-8192, turns U(1000, 4096)'
+                       + (f' // {turn_div}' if turn_div > 1 else ''),
+           'roofline': {'bound': 'fp64', 'achieved': achieved, 'peak': peak, 'unit': 'GFLOP/s',
+                        'frac': achieved / peak if peak else None,
+                        'flops_per_particle_turn': fl,
+                        'flops_basis': 'executed FP64 work (FMA = 2), compiler model',
+                        'reference_flops_per_particle_turn': b.prog.flops,
+                        'frac_reference_expression':
+                            achieved * b.prog.flops / fl / peak if peak else None},
+           'gpu_launches': launches, 'clocks': clk}
+    if plain:
+        b.upload('seed')
+        t0 = time.perf_counter()
+        ms_plain = timed(lambda: b.plain_launches(stream=stream.cuda_stream), 1)
+        fp, lp = b.download()
+        identical = bool(np.array_equal(fb, fp, equal_nan=True) and np.array_equal(lb, lp))
+        out['plain_one_launch_per_seed'] = {'value': pet / (ms_plain / 1e3), 'ms': ms_plain,
+                                            'launches': int(np.sum(b.particles > 0)),
+                                            'wall_s': time.perf_counter() - t0}
+        out['speedup_batched_vs_plain'] = ms_plain / ms_batch
+        out['identical_results'] = identical
+    del b
+    torch.cuda.empty_cache()
+    return out
+
+
+def bench_c4(args):
+    """Batched error seeds (C4) as its own line."""
+    import torch
+    import ufo_gb300 as u
+    torch.cuda.set_device(0)
+    ctx = u.context(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    r = c4_measure(ctx, stream, args.mode, seeds=args.seeds, turn_div=args.turn_div,
+                   reps=args.steps, warmup=args.warmup)
+    line = {'metric': 'FP64 particle*element*turns/s', 'value': r['value'],
             'unit': 'particle*element*turns/s', 'n_gpus': 1, 'steps': args.steps,
-            'warmup': args.warmup, 'ms_per_step': ms_batch, 'higher_is_better': True,
+            'warmup': args.warmup, 'ms_per_step': r['ms_per_launch'], 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
-            'config': {'workload': f'C4 batched error seeds: first {S} of 512 seeds of the C1 '
-                                   f'ring with dx/dy and normal/skew errors of MAD orders 3-6, '
-                                   f'particles log-uniform 256-8192, turns U(1000, 4096) // '
-                                   f'{args.turn_div}', 'particles': b.n, 'seeds': S,
-                       'mode': args.mode, 'tuning': tuning},
-            'roofline': {'bound': 'fp64', 'achieved': achieved, 'peak': peak, 'unit': 'GFLOP/s',
-                         'frac': achieved / peak if peak else None, 'traffic': None,
-                         'flops_per_particle_turn': fl,
-                         'peak_source': 'measured live: ufo_fp64_peak'},
-            'plain_one_launch_per_seed': {'value': pet / (ms_plain / 1e3), 'ms': ms_plain},
-            'speedup_batched_vs_plain': ms_plain / ms_batch,
-            'identical_results': identical, 'gpu_launches': launches}
-    if clk:
-        line['clocks'] = clk
+            'config': {'workload': r['workload'], 'particles': r['particles'],
+                       'seeds': r['seeds'], 'mode': args.mode, 'tuning': r['tuning']},
+            'roofline': dict(r['roofline'], traffic=None,
+                             peak_source='measured live: ufo_fp64_peak'),
+            'plain_one_launch_per_seed': r['plain_one_launch_per_seed'],
+            'speedup_batched_vs_plain': r['speedup_batched_vs_plain'],
+            'identical_results': r['identical_results'], 'gpu_launches': r['gpu_launches']}
+    if r['clocks']:
+        line['clocks'] = r['clocks']
     print(json.dumps(line), flush=True)
 
 
@@ -508,10 +610,10 @@ def bench_c3(args):
                                          max(1, args.steps // 2))
     ms_p, launches, lost_p = runs[('sorted', False)]
     ms_plain, _, lost_plain = runs[('sorted', True)]
-    # the public API: StableAperture.run with and without its two-phase
-    # compaction (host buffers in and out, wall clock)
+    # the public API: StableAperture.run with in-kernel compaction (default),
+    # two-phase compaction and none (host buffers in and out, wall clock)
     api = {}
-    for compact in (False, True):
+    for compact in (False, 'two-phase', True):
         sa = u.StableAperture(ring, flags=flags | u.DOUBLE_PRECISION, turns=T, particles=n,
                               parameters=['x', 'px', 'y', 'py', 'dp'], context=ctx)
         sa.parameters[:] = grid[:, [0, 1, 2, 3, 5]]
@@ -559,27 +661,126 @@ def bench_c3(args):
                 'plain': pet / (runs[('amplitude', True)][0] / 1e3),
                 'note': 'the same grid, largest amplitude (then |dp|) first'},
             'stable_aperture_api': {
-                'one_phase': {'value': pet / api[False][0], 's': api[False][0]},
+                'one_phase_no_compaction': {'value': pet / api[False][0], 's': api[False][0]},
                 'two_phase_compaction': {
-                    'value': pet / api[True][0], 's': api[True][0],
-                    'survivors_after_turns_div_8': api[True][3],
-                    'second_phase_warps_per_sm': api[True][2]},
+                    'value': pet / api['two-phase'][0], 's': api['two-phase'][0],
+                    'survivors_after_turns_div_8': api['two-phase'][3],
+                    'second_phase_warps_per_sm': api['two-phase'][2]},
+                'in_kernel_compaction': {'value': pet / api[True][0], 's': api[True][0]},
                 'note': 'StableAperture.run end to end (host buffers); the two-phase run '
                         'tracks turns/8 on the full grid, then only the survivors on a grid '
-                        'sized to them'},
+                        'sized to them; the default packs survivors inside one launch'},
             'identical_loss_turns': bool(all(np.array_equal(lost_p, r[2])
                                              for r in runs.values()) and
-                                         np.array_equal(api[False][1], lost_p) and
-                                         np.array_equal(api[True][1], lost_p)),
+                                         all(np.array_equal(a[1], lost_p)
+                                             for a in api.values())),
             'gpu_launches': launches,
             'e2e': {'value': pet / api[True][0], 'unit': 'particle*element*turns/s',
                     'h2d_bytes_per_step': n * 6 * 8,
                     'd2h_bytes_per_step': n * (6 * 8 + 4),
-                    'api': 'ufo_gb300.StableAperture(...).run() (two-phase compaction, host '
+                    'api': 'ufo_gb300.StableAperture(...).run() (in-kernel compaction, host '
                            'buffers)'}}
     if clk:
         line['clocks'] = clk
     print(json.dumps(line), flush=True)
+
+
+def c3_measure(ctx, stream, mode, reps=2):
+    """Dynamic-aperture scan (C3) for the default line: the 196,608-particle
+    grid x 2,048 turns with the StableAperture loss test, in one launch of the
+    CTA-compacting persistent kernel, the one-warp persistent kernel and the
+    plain kernel (FMA arithmetic unless ``mode`` is strict), plus one strict
+    launch whose loss turns are the reference's (bit-exact against the oracle
+    in the GPU tests): every variant's loss turns must equal the strict
+    ones.  ``e2e``: StableAperture.run (host buffers, two-phase compaction)."""
+    import torch
+    import ufo_gb300 as u
+    from ufo_gb300 import capi, compiler as C, workloads as W
+    lib = capi.load()
+    dev = torch.device('cuda', ctx.device)
+    ring = W.c3_ring(u)
+    n_elem = len(ring.flatten())
+    grid = W.c3_grid()
+    n, T = grid.shape[0], 2048
+    coords = torch.from_numpy(grid).to(dev)
+    lost = torch.empty(n, dtype=torch.int32, device=dev)
+    final = torch.empty((n, 6), dtype=torch.float64, device=dev)
+    progs = {}
+
+    def launch(m, extra):
+        if m not in progs:
+            progs[m] = capi.DeviceProgram(ctx, C.compile_line(
+                ring, u.KICK | (u.FMA if m == 'fma' else 0), where=[-1]))
+        tf = (capi.UFO_TRACK_FMA if m == 'fma' else 0) | extra
+        capi.check(lib.ufo_track_device(
+            ctx.handle, progs[m].handle, capi.ptr(coords.data_ptr()), None, None, n, T,
+            capi.UFO_MODE_SA, tf, 0, 1, None, capi.ptr(lost.data_ptr()),
+            capi.ptr(final.data_ptr()), capi.ptr(stream.cuda_stream)))
+
+    def timed(m, extra, k):
+        # the compacting kernel with StableAperture's resident warps per SM
+        ctx.set_tuning(u.StableAperture.COMPACT_WARPS_PER_SM
+                       if extra & capi.UFO_TRACK_COMPACT else 16)
+        launch(m, extra)  # warm-up
+        torch.cuda.synchronize()
+        l0 = ctx.launches()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            launch(m, extra)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return (e0.elapsed_time(e1) / k, ctx.launches() - l0,
+                lost.cpu().numpy().view(np.uint32).astype(np.int64))
+
+    ms_strict, _, lost_strict = timed('strict', capi.UFO_TRACK_COMPACT, 1)
+    tracked = float(np.where(lost_strict < T, lost_strict + 1, T).sum())
+    pet = tracked * n_elem
+    variants = {}
+    identical = True
+    for name, extra in (('compact', capi.UFO_TRACK_COMPACT), ('persistent', 0),
+                        ('plain', capi.UFO_TRACK_PLAIN)):
+        ms, launches, lo = timed(mode, extra, reps)
+        identical &= bool(np.array_equal(lo, lost_strict))
+        variants[name] = {'value': pet / (ms / 1e3), 'ms': ms, 'launches': launches}
+    ctx.set_tuning(16)
+    sa = u.StableAperture(ring, flags=u.KICK | (u.FMA if mode == 'fma' else 0) |
+                          u.DOUBLE_PRECISION, turns=T, particles=n,
+                          parameters=['x', 'px', 'y', 'py', 'dp'], context=ctx)
+    sa.parameters[:] = grid[:, [0, 1, 2, 3, 5]]
+    sa.run()  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    sa.run()
+    e2e_s = time.perf_counter() - t0
+    identical &= bool(np.array_equal(sa.lost.astype(np.int64), lost_strict))
+    peak = ctypes_peak(ctx)
+    prog = C.compile_line(ring, u.KICK | (u.FMA if mode == 'fma' else 0), where=[-1])
+    fl = prog.flops_fast if mode == 'fma' else prog.flops
+    best = variants['compact']
+    achieved = fl * tracked / (best['ms'] / 1e3) / 1e9
+    return {
+        'workload': 'C3 dynamic aperture: 256x256 polar grid (r 0-25 mm, angle 0-pi/2) x dp '
+                    '{-2%, 0, +2%} = 196,608 particles, 2,048 turns, SA loss test, C1 ring with '
+                    '10 mm apertures and C4 seed-0 errors',
+        'value': best['value'], 'unit': 'particle*element*turns/s', 'mode': mode,
+        'kernel': 'CTA-compacting persistent kernel, one launch',
+        'ms_per_launch': best['ms'], 'particle_turns_tracked': int(tracked),
+        'survival_fraction': float(np.mean(lost_strict >= T)),
+        'roofline': {'bound': 'fp64', 'achieved': achieved, 'peak': peak, 'unit': 'GFLOP/s',
+                     'frac': achieved / peak if peak else None, 'flops_per_particle_turn': fl,
+                     'flops_basis': 'executed FP64 work (FMA = 2), compiler model',
+                     'reference_flops_per_particle_turn': prog.flops,
+                     'frac_reference_expression':
+                         achieved * prog.flops / fl / peak if peak else None},
+        'variants': variants,
+        'strict_one_launch': {'value': pet / (ms_strict / 1e3), 'ms': ms_strict},
+        'loss_turns_identical_to_strict': identical,
+        'loss_turns_note': 'every variant and the public API give, for all 196,608 particles, '
+                           'the loss turns of the strict (bit-identical) arithmetic',
+        'e2e': {'value': pet / e2e_s, 'unit': 'particle*element*turns/s', 's': e2e_s,
+                'h2d_bytes_per_step': n * 6 * 8, 'd2h_bytes_per_step': n * (6 * 8 + 4),
+                'api': 'ufo_gb300.StableAperture(...).run() (host buffers)'}}
 
 
 def _normwise(g, fd):
@@ -729,7 +930,7 @@ def _c5_multiturn(args, u, W, torch, ctx, stream, model, ring, params, vals, rng
     return out, launches
 
 
-def bench_c5(args):
+def c5_measure(args, ctx, stream):
     """Adjoint gradients (C5: the C2 ring with one error seed, 320 k1 + 192 k2)
     against central finite differences, accuracy over all 512 parameters and
     cost in device time (CUDA events around every kernel) and wall time:
@@ -752,14 +953,12 @@ def bench_c5(args):
     import torch
     import ufo_gb300 as u
     from ufo_gb300 import diff as D, workloads as W
-    torch.cuda.set_device(0)
-    stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)  # every kernel below and its events on one stream
-    ctx = u.context(0)
     ring = W.c5_ring(u)
     params, vals = W.c5_parameters(ring)
     P = len(vals)
-    model = D.OpticsModel(ring, u.KICK, params, h_dp=1e-5)
+    # chromaticity = central difference of the tunes in dp at the reference's
+    # dp step (1e-4, tests/optics3.py)
+    model = D.OpticsModel(ring, u.KICK, params, h_dp=1e-4)
     clocks = Clocks(0)
     clocks.start()
     model.evaluate(vals)  # warm-up
@@ -788,16 +987,19 @@ def bench_c5(args):
     dev_fd = fs[0].device_ms
     launches += fs[0].launches
     Jfd = ((fo[0::2] - fo[1::2]) / (2 * h[:, None])).T
-    rows4, h4 = fd_rows(1e-5, (2, 1, -1, -2))
-    rows4x, h4x = fd_rows(1e-4, (2, 1, -1, -2))
-    f4 = model.evaluate_many(rows4)
-    f4x = model.evaluate_many(rows4x)
-
-    def st4(f, hh):
+    def st4(hrel):
+        r, hh = fd_rows(hrel, (2, 1, -1, -2))
+        f = model.evaluate_many(r)
         return ((-f[0::4] + 8 * f[1::4] - 8 * f[2::4] + f[3::4]) / (12 * hh[:, None])).T
 
-    J4 = st4(f4, h4)
-    J4[6:8] = st4(f4x, h4x)[6:8]
+    def richardson(hrel):  # 4-point stencils at h and 2h: the h^4 term cancels
+        a, b = st4(hrel), st4(2 * hrel)
+        return (16 * a - b) / 15, a
+
+    J4, S4 = richardson(1e-5)
+    J4x, S4x = richardson(1e-3)
+    J4[6:8] = J4x[6:8]
+    S4[6:8] = S4x[6:8]
     names = ['x_co', 'px_co', 'y_co', 'py_co', 'Qx', 'Qy', 'xi_x', 'xi_y']
     res['optics_one_seed'] = {
         'outputs': dict(zip(names, out.tolist())),
@@ -806,6 +1008,9 @@ def bench_c5(args):
         'device_cost_ratio': dev_fd / dev_adj, 'wall_cost_ratio': wall_fd / wall_adj,
         'normwise_rel_err_vs_central_fd_h1e-7': dict(zip(names, _normwise(Jad, Jfd))),
         'normwise_rel_err_vs_4pt_fd': dict(zip(names, _normwise(Jad, J4))),
+        'stencil': 'Richardson-combined 4-point stencils (h, 2h): h = 1e-5 relative for orbit '
+                   'and tunes, 1e-3 for the chromaticities (dp difference at 1e-4)',
+        'stencil_own_error_estimate': dict(zip(names, _normwise(S4, J4))),
         'note': 'one seed leaves the GPU mostly idle: the 3,072 FD Newton jobs run '
                 'beside each other in the time of the 3 adjoint jobs'}
 
@@ -844,19 +1049,62 @@ def bench_c5(args):
     ratios = [res['optics_batched']['device_cost_ratio']]
     if res.get('multiturn'):
         ratios.append(res['multiturn']['device_cost_ratio'])
-    ratio = min(ratios)
+    res['device_cost_ratio_min'] = min(ratios)
+    res['gpu_launches'] = launches
+    res['clocks'] = clk
+    return res
+
+
+def bench_c5(args):
+    """Adjoint gradients (C5) as its own line."""
+    import torch
+    import ufo_gb300 as u
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)  # every kernel below and its events on one stream
+    ctx = u.context(0)
+    res = c5_measure(args, ctx, stream)
     line = {'metric': 'adjoint gradient cost advantage over central finite differences '
                       '(device time, all 512 parameters)',
-            'value': ratio, 'unit': 'x', 'n_gpus': 1, 'steps': 1, 'warmup': 1,
-            'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
-            'data': 'synthetic',
-            'config': {'workload': 'C5 adjoint optics gradients: C2 ring (1024 elements) with '
-                                   'one error seed, d/d(320 k1 + 192 k2) of closed orbit, '
-                                   'tunes, chromaticity; 4096-particle 1024-turn amplitude '
-                                   'adjoint with checkpoints every 64 turns'},
-            'gpu_launches': launches, 'clocks': clk}
+            'value': res.pop('device_cost_ratio_min'), 'unit': 'x', 'n_gpus': 1, 'steps': 1,
+            'warmup': 1, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+            'dtype': 'f64', 'data': 'synthetic',
+            'config': {'workload': C5_WORKLOAD},
+            'gpu_launches': res.pop('gpu_launches'), 'clocks': res.pop('clocks')}
     line.update(res)
     print(json.dumps(line), flush=True)
+
+
+def c5_summary(res):
+    """The C5 object of the default line: cost ratios and accuracy over all
+    512 strengths (details in ``--workload c5``)."""
+    one, bat = res['optics_one_seed'], res['optics_batched']
+    out = {'workload': C5_WORKLOAD,
+           'value': res['device_cost_ratio_min'], 'unit': 'x (FD device time / adjoint)',
+           'optics_jacobian_8x512': {
+               'device_cost_ratio_batched': bat['device_cost_ratio'],
+               'wall_cost_ratio_batched': bat['wall_cost_ratio'],
+               'device_cost_ratio_one_seed': one['device_cost_ratio'],
+               'max_normwise_rel_err_vs_stencil': max(one['normwise_rel_err_vs_4pt_fd'].values()),
+               'normwise_rel_err_vs_stencil': one['normwise_rel_err_vs_4pt_fd'],
+               'normwise_rel_err_vs_central_fd_h1e-7':
+                   one['normwise_rel_err_vs_central_fd_h1e-7'],
+               'stencil': one.get('stencil')},
+           'gpu_launches': res['gpu_launches'], 'clocks': res['clocks']}
+    mt = res.get('multiturn')
+    if mt:
+        out['multiturn_4096x1024'] = {
+            k: mt[k] for k in ('device_cost_ratio', 'adjoint_device_ms',
+                               'fd_all_params_device_ms_scaled', 'regular_particles',
+                               'max_rel_err_vs_4pt_stencil_same_map',
+                               'stencil_steps_disagreement',
+                               'max_rel_err_vs_central_fd_h1e-7') if k in mt}
+    return out
+
+
+C5_WORKLOAD = ('C5 adjoint optics gradients: C2 ring (1024 elements) with one error seed, '
+               'd/d(320 k1 + 192 k2) of closed orbit, tunes, chromaticity; 4096-particle '
+               '1024-turn amplitude adjoint with checkpoints every 64 turns')
 
 
 def ctypes_peak(ctx):
@@ -885,10 +1133,48 @@ def fp64_probe():
     print(json.dumps({'fp64_probe': rows, 'fp64_peak_gflops': ctypes_peak(ctx)}), flush=True)
 
 
+def op_mix():
+    """One small launch per element type and arithmetic mode (strict, FMA):
+    64 identical elements, 4,096 particles, 10 turns each -- the command an
+    ncu capture of the FP64 instruction mix per element type runs (counts per
+    launch / (4,096 x 10 x 64) = per particle and element)."""
+    import math
+    import ufo_gb300 as u
+    from ufo_gb300 import capi, compiler as C, workloads as W
+    ctx = u.context(0)
+    n, T = 4096, 10
+    beam = W.c2_beam(n, seed=6)
+    lines = {
+        'drift': [u.Drift(f'd{i}', length=1.0) for i in range(64)],
+        'quad': [u.Quadrupole(f'q{i}', length=0.25, k1=1.2 * (-1) ** i, slices=4)
+                 for i in range(64)],
+        'sext': [u.Sextupole(f's{i}', length=0.2, k2=40.0 * (-1) ** i, slices=4)
+                 for i in range(64)],
+        'bend': [u.Sbend(f'b{i}', length=1.38, angle=2 * math.pi / 128, slices=4)
+                 for i in range(64)],
+    }
+    out = []
+    for name, elems in lines.items():
+        line = u.Line(name, elems)
+        for mode in ('strict', 'fma'):
+            prog = C.compile_line(line, u.KICK | (u.FMA if mode == 'fma' else 0), where=[-1])
+            dp = capi.DeviceProgram(ctx, prog)
+            capi.track(ctx, dp, beam, T, capi.UFO_MODE_TRACK,
+                       capi.UFO_TRACK_FMA if mode == 'fma' else 0, slots=0)
+            out.append({'type': name, 'mode': mode, 'elements': 64, 'particles': n, 'turns': T,
+                        'ops_per_turn': len(prog.ops),
+                        'reference_flops_per_element': prog.flops / 64,
+                        'fma_flops_per_element': prog.flops_fast / 64})
+    print(json.dumps({'op_mix_launches': out}), flush=True)
+
+
 def main():
     args = parse()
     if args.fp64_probe:
         fp64_probe()
+        return
+    if args.op_mix:
+        op_mix()
         return
     if args.impl == 'reference':
         bench_reference(args)

@@ -38,6 +38,7 @@ extern "C" {
 #define UFO_TRACK_FMA 1      /* fused multiply-add arithmetic (tolerance parity) */
 #define UFO_TRACK_FIVED 2    /* do not write z, dp into tracks (ufo/track.py:62-65) */
 #define UFO_TRACK_PLAIN 4    /* one thread per particle, no lane refill */
+#define UFO_TRACK_COMPACT 8  /* persistent CTAs that pack survivors into full warps */
 
 #define UFO_OP_WORDS 8
 

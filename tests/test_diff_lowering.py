@@ -21,7 +21,18 @@ def interpret(dprog, z, o, turns=1, seed=0):
                 x, y = x - c[0], y - c[1]
             elif kind == D.D_EDGE:
                 curv = c[0] * oo
-                px, py = px + x * curv * c[1], py - y * curv * c[2]
+                t2 = np.tan(c[2] - 2 * curv * c[3] / c[4] * c[5]) if _fl & D.DE_RTPSI else c[2]
+                px, py = px + x * curv * c[1], py - y * curv * t2
+            elif kind == D.D_THICK:
+                L, k1, h = c[0], c[1], c[2]
+                bend = _fl & D.DT_BEND
+                Kx = oo * (k1 + h * h)
+                Ky = -oo * k1
+                Cx, Sx, D1x, _, _, _ = D.thick_functions(Kx, L)
+                Cy, Sy, _, _, _, _ = D.thick_functions(Ky, L)
+                disp = (1 / o - 1) * h * oo if bend else 0.0
+                x, px = Cx * x + Sx * px + disp * D1x, -Kx * Sx * x + Cx * px + disp * Sx
+                y, py = Cy * y + Sy * py, -Ky * Sy * y + Cy * py
             elif kind in (D.D_TEAPOT, D.D_KICK):
                 tp = kind == D.D_TEAPOT
                 n = N if tp else 1
@@ -55,7 +66,8 @@ def _c5():
     return W.c5_ring(u)
 
 
-@pytest.mark.parametrize('which', ['c5_kick', 'c2_linear'])
+@pytest.mark.parametrize('which', ['c5_kick', 'c2_linear', 'c5_thick', 'alba_thick',
+                                   'alba_thick_achromatic'])
 def test_lowered_program_matches_oracle(which):
     import ufo_gb300 as u
     from ufo_gb300 import diff as D
@@ -65,12 +77,48 @@ def test_lowered_program_matches_oracle(which):
         coords = np.array([[1e-3, 1e-4, -5e-4, 2e-5, 0, 1e-3],
                            [-2e-4, 3e-5, 1e-4, -1e-5, 0, -2e-3],
                            [0, 0, 0, 0, 0, 0]])
-    else:
+    elif which == 'c2_linear':
         ring, flags = _linear_ring(), u.KICK | u.LINEAR
         coords = np.array([[1.0, 0, 1.0, 0, 0, 0], [0, 1.0, 0, 1.0, 0, 0],
                            [1e-3, 0, 0, 0, 0, 1e-4], [0, 0, 0, 0, 0, 0]])
+    else:  # exact thick quadrupoles and sector bends (the reference's default)
+        import os
+        if which == 'c5_thick':
+            ring, flags = _c5(), 0
+        else:
+            import helpers as H
+            ring = u.Lattice(path=os.path.join(H.HERE, 'golden', 'madx', 'alba.mad')).RING
+            flags = u.ACHROMATIC if which == 'alba_thick_achromatic' else 0
+        coords = np.array([[1e-3, 1e-4, -5e-4, 2e-5, 0, 1e-3],
+                           [-2e-4, 3e-5, 1e-4, -1e-5, 0, -2e-3],
+                           [0, 0, 0, 0, 0, 0]])
     dp = D.DiffProgram(ring, flags, [])
     got = interpret(dp, coords[:, :4], 1 / (1 + coords[:, 5]))
     ref = O.track(ring, flags | u.DOUBLE_PRECISION, coords, 1, tracks=False)['final'][:, :4]
     scale = np.maximum(np.abs(ref).max(axis=0), 1e-300)
     assert np.all(np.abs(got - ref) <= 1e-12 * scale + 1e-18), (got - ref)
+
+
+def test_thick_functions_and_their_derivatives():
+    """thick_functions: the closed forms against the series across the switch
+    at |K L^2| = 1, both signs of K, and the K-derivatives against central
+    differences."""
+    from ufo_gb300 import diff as D
+    L = 0.7
+    K = np.array([-30.0, -2.05, -2.0408, -0.5, -1e-9, 1e-9, 0.3, 2.0408, 2.05, 40.0])
+    C, Sw, D1, dC, dSw, dD1 = D.thick_functions(K, L)
+    w = np.sqrt(np.abs(K).astype(np.longdouble))
+    Cr = np.where(K > 0, np.cos(w * L), np.cosh(w * L))
+    Sr = np.where(K > 0, np.sin(w * L), np.sinh(w * L)) / w
+    np.testing.assert_allclose(C, Cr.astype(float), rtol=1e-14, atol=1e-15)
+    np.testing.assert_allclose(Sw, Sr.astype(float), rtol=1e-14)
+    big = np.abs(K) > 1e-3
+    np.testing.assert_allclose(D1[big], ((1 - Cr) / K)[big].astype(float), rtol=1e-12)
+    for f, df in ((0, dC), (1, dSw), (2, dD1)):
+        h = 1e-5 * np.maximum(np.abs(K), 1.0)
+        fp = D.thick_functions(K + h, L)[f]
+        fm = D.thick_functions(K - h, L)[f]
+        fp2 = D.thick_functions(K + 2 * h, L)[f]
+        fm2 = D.thick_functions(K - 2 * h, L)[f]
+        fd = (-fp2 + 8 * fp - 8 * fm + fm2) / (12 * h)
+        np.testing.assert_allclose(df, fd, rtol=1e-8, atol=1e-12)

@@ -82,6 +82,180 @@ def test_optics_gradients_match_central_differences(which, h_rel, tol):
         assert abs(gi - fdi) <= tol * max(abs(fdi), 1e-6 * scale) + eps / (2 * hi), (i, gi, fdi)
 
 
+def _stencil4(model, vals, hrel, idx=None):
+    """Jacobian columns by the 4-point stencil (f(k-2h) - 8 f(k-h) + 8 f(k+h)
+    - f(k+2h)) / 12h at relative step ``hrel`` (truncation ~h^4, rounding noise
+    ~eps/h): [8, len(idx)]."""
+    idx = np.arange(len(vals)) if idx is None else np.asarray(idx)
+    m = len(idx)
+    h = hrel * np.abs(vals[idx])
+    rows = np.repeat(vals[None], 4 * m, axis=0)
+    for q, cst in enumerate((2.0, 1.0, -1.0, -2.0)):
+        rows[q::4][np.arange(m), idx] += cst * h
+    f = model.evaluate_many(rows)
+    return ((-f[0::4] + 8 * f[1::4] - 8 * f[2::4] + f[3::4]) / (12 * h[:, None])).T
+
+
+def _richardson(model, vals, hrel, idx=None):
+    """Two 4-point stencils at h and 2h combined to cancel the h^4 term
+    (error ~h^6); and the difference between the two stencils' estimates."""
+    a = _stencil4(model, vals, hrel, idx)
+    b = _stencil4(model, vals, 2 * hrel, idx)
+    return (16 * a - b) / 15, a
+
+
+def _normwise(J, R):
+    return np.max(np.abs(J - R), axis=1) / np.max(np.abs(R), axis=1)
+
+
+def test_optics_jacobian_within_1e7_of_accurate_differences():
+    """The whole 8 x 512 Jacobian (closed orbit, tunes, chromaticities with
+    respect to all 320 k1 and 192 k2 of the C5 ring) from one adjoint pass,
+    against finite differences accurate well below 1e-7: Richardson-combined
+    4-point stencils, at h = 1e-5 (relative) for orbit and tunes and h = 1e-3
+    for the chromaticities.  The chromaticity is itself a central difference
+    of the tunes in dp (step 1e-4, the reference's dp step in
+    tests/optics3.py); its rounding noise, divided by a small k step, would
+    swamp a small-step difference.  Bar: normwise relative error <= 1e-7 on
+    every output row.  The differences' own error is bounded by comparing the
+    Richardson estimate with the plain stencil at the smaller step."""
+    import ufo_gb300 as u
+    from ufo_gb300 import diff as D
+    ring = _ring()
+    params, vals = _params(ring)
+    model = D.OpticsModel(ring, u.KICK, params, h_dp=1e-4)
+    out, saved = model.evaluate(vals)
+    J = model.vjp(saved, np.eye(8))
+    Ro, So = _richardson(model, vals, 1e-5)
+    Rx, Sx = _richardson(model, vals, 1e-3)
+    R = np.concatenate([Ro[:6], Rx[6:]])
+    err = _normwise(J, R)
+    assert np.all(err <= 1e-7), err
+    own = np.concatenate([_normwise(So, Ro)[:6], _normwise(Sx, Rx)[6:]])
+    assert np.all(own <= 1e-7), own
+
+
+def _thick_alba():
+    import os
+    import ufo_gb300 as u
+    import helpers as H
+    ring = u.Lattice(path=os.path.join(H.HERE, 'golden', 'madx', 'alba.mad')).RING
+    flat = ring.flatten()
+    params, vals = [], []
+    for i, e in enumerate(flat):
+        if type(e).__name__ == 'Quadrupole':
+            params.append((i, 'k1'))
+            vals.append(e.k1)
+    return ring, params, np.array(vals)
+
+
+def test_thick_alba_tune_gradients_within_1e7():
+    """The reference's default model: the ALBA ring with exact thick
+    quadrupoles and sector bends (no KICK; fringe-field edges whose angle
+    depends on dp).  dQx/dk1, dQy/dk1 over every quadrupole, and the
+    chromaticity gradients, from the adjoint against Richardson-combined
+    4-point stencils: <= 1e-7 normwise."""
+    from ufo_gb300 import diff as D
+    ring, params, vals = _thick_alba()
+    model = D.OpticsModel(ring, 0, params, h_dp=1e-4)
+    out, saved = model.evaluate(vals)
+    assert 0 < out[4] < 1 and 0 < out[5] < 1
+    J = model.vjp(saved, np.eye(8))
+    Ro, _ = _richardson(model, vals, 1e-5)
+    Rx, _ = _richardson(model, vals, 1e-3)
+    err = _normwise(J[4:6], Ro[4:6])
+    assert np.all(err <= 1e-7), err
+    errx = _normwise(J[6:8], Rx[6:8])
+    assert np.all(errx <= 1e-7), errx
+
+
+def test_thick_tunes_match_the_optics_driver():
+    """The differentiator's thick maps give the tunes of the Optics driver
+    (the reference's unit-particle method through the tracking kernels) on
+    the thick ALBA ring, chromatic and achromatic."""
+    import ufo_gb300 as u
+    from ufo_gb300 import diff as D
+    ring, params, vals = _thick_alba()
+    for flags in (0, u.ACHROMATIC):
+        out, _ = D.OpticsModel(ring, flags, params).evaluate(vals)
+        o = u.Optics(ring, flags=u.LINEAR | flags | u.DOUBLE_PRECISION)
+        o.run()
+        assert abs(out[4] - o.qx) < 1e-10 and abs(out[5] - o.qy) < 1e-10, (out[4:6], o.qx, o.qy)
+
+
+def test_thick_multiturn_adjoint_matches_stencil():
+    """Multi-turn amplitude adjoint through thick quadrupoles and bends (C5
+    ring without KICK, 256 particles x 256 turns, checkpoints every 32)
+    against a 4-point stencil of the same map: <= 1e-7."""
+    import torch
+    import ufo_gb300 as u
+    from ufo_gb300 import diff as D, workloads as W
+    ring = _ring()
+    params, vals = _params(ring)
+    model = D.OpticsModel(ring, 0, params)
+    coords = W.c2_beam(256, seed=3)
+    k = torch.tensor(vals, dtype=torch.float64, requires_grad=True)
+    a = D.amplitudes(k, model, coords, 256, ck=32)
+    a.sum().backward()
+    g = k.grad.numpy()
+    idx = np.sort(np.random.default_rng(4).choice(len(vals), 8, replace=False))
+    o = 1 / (1 + coords[:, 5])
+    fd = []
+    for hr in (1e-6, 2e-6):
+        h = hr * np.abs(vals[idx])
+        rows = np.repeat(vals[None], 32, axis=0)
+        for q, cst in enumerate((2.0, 1.0, -1.0, -2.0)):
+            rows[q::4][np.arange(8), idx] += cst * h
+        eng = D.DiffEngine(D.DiffProgram(ring, 0, params, rows))
+        z, _ = eng.forward(np.tile(coords[:, :4], (32, 1)), np.tile(o, 32), 256,
+                           seed=np.repeat(np.arange(32, dtype=np.int32), 256))
+        f = (z[:, 0] ** 2 + z[:, 2] ** 2).reshape(32, 256).sum(axis=1)
+        fd.append((-f[0::4] + 8 * f[1::4] - 8 * f[2::4] + f[3::4]) / (12 * h))
+    R = (16 * fd[0] - fd[1]) / 15
+    err = np.max(np.abs(g[idx] - R)) / np.max(np.abs(R))
+    assert err <= 1e-7, (err, g[idx], R)
+
+
+def test_multiturn_1024_turns_within_1e7_of_stencil():
+    """The 1,024-turn amplitude adjoint (C5 ring, 512 beam particles,
+    checkpoints every 64 turns) over the regular particles (final state moves
+    by less than 200x a 1e-9 m start displacement) against a 4-point stencil of
+    the same map at h = 5e-7 (relative; its truncation ~h^4 and rounding
+    noise ~eps/h balance there): normwise <= 1e-7 over 8 sampled strengths."""
+    import ufo_gb300 as u
+    from ufo_gb300 import diff as D, workloads as W
+    ring = _ring()
+    params, vals = _params(ring)
+    model = D.OpticsModel(ring, u.KICK, params)
+    Np, T = 512, 1024
+    coords = W.c2_beam(Np, seed=3)
+    o = 1.0 / (coords[:, 5] + 1.0)
+    eng = model.engine(vals)
+    pair = np.concatenate([coords[:, :4], coords[:, :4] + [1e-9, 0, 0, 0]])
+    zp, _ = eng.forward(pair, np.concatenate([o, o]), T)
+    growth = np.max(np.abs(zp[Np:, :4] - zp[:Np, :4]), axis=1) / 1e-9
+    reg = growth < 200
+    assert reg.sum() >= 0.95 * Np
+    zT, st = eng.forward(coords[:, :4], o, T, ck=64)
+    zbar = np.zeros((Np, 4))
+    zbar[:, 0] = 2 * zT[:, 0] * reg
+    zbar[:, 2] = 2 * zT[:, 2] * reg
+    _, gp = eng.reverse(st, zbar)
+    g = gp.sum(axis=0)
+    idx = np.sort(np.random.default_rng(1).choice(len(vals), 8, replace=False))
+    h = 5e-7 * np.abs(vals[idx])
+    rows = np.repeat(vals[None], 32, axis=0)
+    for q, cst in enumerate((2.0, 1.0, -1.0, -2.0)):
+        rows[q::4][np.arange(8), idx] += cst * h
+    e4 = D.DiffEngine(D.DiffProgram(ring, u.KICK, params, rows))
+    z4, _ = e4.forward(np.tile(coords[:, :4], (32, 1)), np.tile(o, 32), T,
+                       seed=np.repeat(np.arange(32, dtype=np.int32), Np))
+    f = ((z4[:, 0] ** 2 + z4[:, 2] ** 2).reshape(32, Np) * reg[None]).sum(axis=1)
+    fd = (-f[0::4] + 8 * f[1::4] - 8 * f[2::4] + f[3::4]) / (12 * h)
+    err = np.max(np.abs(g[idx] - fd)) / np.max(np.abs(fd))
+    assert err <= 1e-7, (err, g[idx], fd)
+
+
 def test_multiturn_amplitude_adjoint_matches_differences():
     import torch
     import ufo_gb300 as u

@@ -193,22 +193,24 @@ def test_c3_full_grid_subset_loss_turns_vs_oracle():
 
 def test_stable_aperture_two_phase_is_identical():
     """StableAperture's compaction (first turns/8 on the full grid, the
-    survivors on a grid sized to them) gives the loss turns and coordinates of
-    one run, bit for bit, in strict and FMA modes."""
+    survivors on a grid sized to them) and its in-kernel compaction (the
+    default) give the loss turns and coordinates of one plain persistent run,
+    bit for bit, in strict and FMA modes."""
     import ufo_gb300 as u
     from ufo_gb300 import workloads as W
     ring = W.c3_ring(u)
     grid = W.c3_grid(48, 48)
     for flags in (u.KICK | u.DOUBLE_PRECISION, u.KICK | u.FMA | u.DOUBLE_PRECISION):
         out = []
-        for compact in (False, True):
+        for compact in (False, 'two-phase', True):
             sa = u.StableAperture(ring, flags=flags, turns=600, particles=len(grid),
                                   parameters=['x', 'px', 'y', 'py', 'dp'])
             sa.parameters[:] = grid[:, [0, 1, 2, 3, 5]]
             sa.run(compact=compact)
             out.append((sa.lost.copy(), sa.final.copy()))
-        assert np.array_equal(out[0][0], out[1][0])
-        assert np.array_equal(out[0][1], out[1][1], equal_nan=True)
+        for lost, final in out[1:]:
+            assert np.array_equal(out[0][0], lost)
+            assert np.array_equal(out[0][1], final, equal_nan=True)
         assert 0 < np.sum(out[0][0] < 600) < len(grid)
 
 
@@ -361,3 +363,147 @@ def test_closed_orbit_parameter_batch():
             assert np.array_equal(co.orbits, ref)
         else:
             assert np.max(np.abs(co.orbits - ref)) < 1e-8
+
+
+@pytest.mark.parametrize('name', ['alba_kick_params', 'alba_thick_params'])
+def test_parameter_rerun_reuses_the_program(name):
+    """The reference's workflow: one simulation object, new lattice values in
+    ``.parameters`` between runs.  The second run takes the set-table path (the
+    device program object is the same; only the per-seed constants are
+    re-uploaded) and reproduces the reference's golden tracks."""
+    c = H.case(name)
+    import ufo_gb300 as u
+    line = H.line_of(c)
+    params = H.latjson.params_load(c['parameters'])
+    pool = H.arr(name, 'in/pool')
+    t = u.Track(line, flags=c['flags'], turns=c['turns'], particles=pool.shape[0],
+                parameters=params, where=c['where'], dp=c.get('dp', 0.0))
+    lat = [j for j, p in enumerate(params) if isinstance(p, tuple)]
+    assert lat
+    first = pool.copy()
+    first[:, lat] *= 1.5  # other lattice values, same zero pattern
+    t.parameters[:] = first
+    t.run()
+    dprog = t._c._dprog
+    before = t.tracks.copy()
+    t.parameters[:] = pool
+    t.run()
+    assert t._c._dprog is dprog
+    ref = H.arr(name, 'out/tracks')
+    assert not np.array_equal(before, ref, equal_nan=True)
+    if H.program_is_exact(t.program):
+        assert np.array_equal(t.tracks, ref, equal_nan=True)
+    else:
+        _assert_within_tolerance(c, t.tracks, ref)
+
+
+def test_c3_full_grid_fma_loss_turns_equal_strict():
+    """Survival masks and loss turns of the whole dynamic-aperture benchmark
+    (196,608 particles x 2,048 turns, C1 ring with apertures and errors) in
+    FMA mode are the strict mode's, particle for particle; strict mode is the
+    reference's arithmetic (bit-exact against the oracle above).  So the FMA
+    throughput figures of this scan come with the reference's loss turns."""
+    import ufo_gb300 as u
+    from ufo_gb300 import capi, compiler as C, workloads as W
+    ring = W.c3_ring(u)
+    grid = W.c3_grid()
+    ctx = u.context(0)
+    ds = capi.DeviceProgram(ctx, C.compile_line(ring, u.KICK, where=[-1]))
+    df = capi.DeviceProgram(ctx, C.compile_line(ring, u.KICK | u.FMA, where=[-1]))
+    _, ls, _ = capi.track(ctx, ds, grid, 2048, capi.UFO_MODE_SA, 0, slots=0)
+    _, lf, _ = capi.track(ctx, df, grid, 2048, capi.UFO_MODE_SA, capi.UFO_TRACK_FMA, slots=0)
+    assert 0 < np.sum(ls < 2048) < len(grid)
+    assert np.array_equal(lf, ls), int(np.sum(lf != ls))
+
+
+@pytest.mark.parametrize('fma', [False, True])
+def test_compacting_kernel_is_bit_identical(fma):
+    """The CTA-compacting persistent kernel (survivors packed into the lowest
+    warps of each CTA once the work counter is exhausted) moves particle
+    states between lanes only: loss turns and final coordinates equal the
+    one-warp persistent kernel's and the plain kernel's bit for bit, on an
+    uneven dynamic-aperture grid and on a batch of error seeds with uneven
+    particle and turn counts."""
+    import ufo_gb300 as u
+    from ufo_gb300 import capi, compiler as C, workloads as W
+    ctx = u.context(0)
+    fl = (u.FMA if fma else 0)
+    tf = capi.UFO_TRACK_FMA if fma else 0
+    ring = W.c3_ring(u)
+    grid = W.c3_grid(96, 96)
+    dp = capi.DeviceProgram(ctx, C.compile_line(ring, u.KICK | fl, where=[-1]))
+    runs = [capi.track(ctx, dp, grid, 700, capi.UFO_MODE_SA, tf | extra, slots=0)
+            for extra in (0, capi.UFO_TRACK_COMPACT, capi.UFO_TRACK_PLAIN)]
+    assert 0 < np.sum(runs[0][1] < 700) < len(grid)
+    for _, lost, final in runs[1:]:
+        assert np.array_equal(lost, runs[0][1])
+        assert np.array_equal(final, runs[0][2], equal_nan=True)
+    # error seeds, uneven particles and turns, fewer warps than one CTA holds
+    ring1 = W.c1_ring(u)
+    params = W.c4_parameters(ring1)
+    rows = W.c4_seed_rows(ring1, 5)
+    prog = C.compile_line(ring1, u.KICK | fl, params, [], seed_values=rows)
+    dq = capi.DeviceProgram(ctx, prog)
+    parts = np.array([37, 300, 5, 64, 211])
+    seed = np.repeat(np.arange(5), parts).astype(np.int32)
+    pturns = np.repeat(np.array([90, 7, 150, 0, 41]), parts).astype(np.int32)
+    beam = W.c1_beam(int(parts.sum()), seed=12)
+    out = [capi.track(ctx, dq, beam, 150, capi.UFO_MODE_TRACK, tf | extra, seed=seed,
+                      pturns=pturns, slots=0) for extra in (0, capi.UFO_TRACK_COMPACT)]
+    assert np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][2], out[1][2], equal_nan=True)
+    assert np.array_equal(out[0][1], pturns)  # nothing is lost in the C1 ring
+
+
+def test_stable_aperture_with_turn_dependent_kicker_runs_in_one_phase():
+    """A time-dependent element (the HOWTO's gate kicker, firing on turn 20)
+    reads ``turn``: StableAperture must not restart turn numbers in a second
+    phase, so a two-phase request runs the in-kernel compaction instead, and
+    every variant equals the plain one-launch run."""
+    import ufo_gb300 as u
+    import kickers
+    from ufo_gb300 import workloads as W
+    ring = W.c3_ring(u)
+    kick = kickers.NLKGate('nlk', knl=[0.0, 0.0, 0.0], ksl=[0.0])
+    kick.knl[1] = 0.5
+    line = u.Line('ring', [kick] + list(ring.flatten()))
+    grid = W.c3_grid(80, 80)
+    out = []
+    for compact in (None, 'two-phase', False):
+        sa = u.StableAperture(line, flags=u.KICK | u.DOUBLE_PRECISION, turns=520,
+                              particles=len(grid), parameters=['x', 'px', 'y', 'py', 'dp'])
+        assert sa._uses_turn()
+        sa.parameters[:] = grid[:, [0, 1, 2, 3, 5]]
+        sa.run(compact=compact)
+        out.append(sa.lost.copy())
+    assert np.array_equal(out[0], out[1]) and np.array_equal(out[0], out[2])
+    assert 0 < np.sum(out[0] < 520) < len(grid)
+
+
+@pytest.mark.parametrize('yoshida', [False, True])
+def test_power_series_kicks_are_bit_identical(yoshida):
+    """FMA programs give general kicks a dense power series prepared on the
+    host (F_PSER): the kernels load the products RN(kn * RN(1/n!)) they would
+    otherwise form at every order.  The same program with the flag cleared
+    takes the per-order path; both give the same bits (error seeds of orders
+    3-6 on every magnet, teapot and Yoshida slices, plain thin kicks)."""
+    import types
+    import ufo_gb300 as u
+    from ufo_gb300 import capi, compiler as C, workloads as W
+    ctx = u.context(0)
+    ring = W.c1_ring(u)
+    extra = [u.Multipole('m', knl=[0.0, 0.0, 3.0, 10.0, 1e3, 1e5], ksl=[0.0, 0.1, 0.0, 5.0])]
+    line = u.Line('l', list(ring.flatten()) + extra)
+    params = W.c4_parameters(ring)
+    rows = W.c4_seed_rows(ring, 4)
+    fl = u.KICK | u.FMA | (u.YOSHIDA if yoshida else 0)
+    prog = C.compile_line(line, fl, params, [], seed_values=rows)
+    assert any(int(r[1]) & C.F_PSER for r in prog.ops)
+    plain = types.SimpleNamespace(ops=prog.ops.copy(), table=prog.table, n_dumps=prog.n_dumps)
+    plain.ops[:, 1] &= ~C.F_PSER
+    beam = W.c1_beam(3000, seed=21)
+    seed = (np.arange(3000) % 4).astype(np.int32)
+    out = [capi.track(ctx, capi.DeviceProgram(ctx, p), beam, 60, capi.UFO_MODE_TRACK,
+                      capi.UFO_TRACK_FMA, seed=seed, slots=0) for p in (prog, plain)]
+    assert np.array_equal(out[0][2], out[1][2], equal_nan=True)
+    assert np.array_equal(out[0][1], out[1][1])

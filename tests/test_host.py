@@ -152,8 +152,9 @@ def test_flop_counts():
 
 def test_fma_drift_merging_conserves_length_and_flops():
     """FMA programs fold plain drifts into neighbouring teapot outer drifts:
-    the total drift length per turn, the element count and the (reference)
-    flop count are unchanged, and strict programs are not touched."""
+    the total drift length per turn, the element count and the reference
+    flop count are unchanged, the executed count drops by the merged drifts'
+    two FMAs each, and strict programs are not touched."""
     import numpy as np
     import ufo_gb300 as u
     from ufo_gb300 import compiler as C, workloads as W
@@ -181,8 +182,65 @@ def test_fma_drift_merging_conserves_length_and_flops():
         strict = C.compile_line(ring, u.KICK, where=[-1])
         fma = C.compile_line(ring, u.KICK | u.FMA, where=[-1])
         assert len(fma.ops) < len(strict.ops)
-        assert fma.flops_fast == strict.flops_fast and fma.n_elements == strict.n_elements
+        merged = sum(int(r[0]) == C.OP_DRIFT for r in strict.ops) - \
+            sum(int(r[0]) == C.OP_DRIFT for r in fma.ops)
+        assert merged > 0
+        assert fma.flops == strict.flops and fma.n_elements == strict.n_elements
+        assert fma.flops_fast == strict.flops_fast - 4 * merged
         assert abs(drift_length(fma) - drift_length(strict)) < 1e-9 * drift_length(strict)
     assert not np.any(C.compile_line(W.c2_ring(u), u.KICK | u.FMA, where=[-1]).ops[:, 0] ==
                       C.OP_DRIFT)
     assert not np.any(C.compile_line(W.c2_ring(u), u.KICK, where=[-1]).ops[:, 1] & C.F_SPLITO)
+
+
+def test_fma_programs_append_dense_power_series_for_general_kicks():
+    """FMA programs append to every general kick (here: C4-style errors of
+    orders 3-6 on every magnet) the dense series a_n = RN(kn_n * RN(1/n!)),
+    then b_n, n up to the highest order, structural zeros as +0.0, after all
+    other constants (F_PSER); quadrupole/sextupole short forms and strict
+    programs get none."""
+    import math
+    import numpy as np
+    import ufo_gb300 as u
+    from ufo_gb300 import compiler as C, workloads as W
+    ring = W.c1_ring(u)
+    params = W.c4_parameters(ring)
+    rows = W.c4_seed_rows(ring, 3)
+    fma = C.compile_line(ring, u.KICK | u.FMA, params, [], seed_values=rows)
+    strict = C.compile_line(ring, u.KICK, params, [], seed_values=rows)
+    assert not any(int(r[1]) & C.F_PSER for r in strict.ops)
+    rf = []
+    fact = 1.0
+    for k in range(8):
+        if k:
+            fact *= float(k)
+        rf.append(1.0 / fact)
+    n_series = 0
+    for r in fma.ops:
+        kind, fl = int(r[0]), int(r[1])
+        if kind != C.OP_TEAPOT:
+            continue
+        N, nn, ns, mn, ms = (int(v) for v in r[3:8])
+        general = ms or not ((nn == 2 and mn == 2) or (nn == 3 and mn == 4) or mn == 0)
+        assert bool(fl & C.F_PSER) == bool(general and (mn | ms))
+        if not fl & C.F_PSER:
+            continue
+        n_series += 1
+        fi = (fl >> C.SH_FINNER) & 3
+        first = int(r[2]) + 1 + (0 if N <= 1 else 4 if fi == C.DF_DIV else 1)
+        tail = int(r[2]) + (first - int(r[2])) + bin(mn).count('1') + bin(ms).count('1') + \
+            (1 if fl & C.F_WEAK else 0) + (1 if fl & C.F_SPLITO else 0)
+        M = (mn | ms).bit_length()
+        coef = fma.table[:, first:first + bin(mn).count('1') + bin(ms).count('1')]
+        ser = fma.table[:, tail:tail + 2 * M]
+        q = 0
+        for part, mask in ((0, mn), (1, ms)):
+            for j in range(M):
+                got = ser[:, part * M + j]
+                if mask >> j & 1:
+                    assert np.array_equal(got, coef[:, q] * rf[j])
+                    q += 1
+                else:
+                    assert np.all(got == 0.0) and not np.any(np.signbit(got))
+    assert n_series > 0
+    assert math.isclose(rf[5], 1 / 120, rel_tol=1e-15)

@@ -14,7 +14,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SO = os.path.join(HERE, 'lib', 'libufo_gb300.so')
 
 UFO_MODE_TRACK, UFO_MODE_SA = 0, 1
-UFO_TRACK_FMA, UFO_TRACK_FIVED, UFO_TRACK_PLAIN = 1, 2, 4
+UFO_TRACK_FMA, UFO_TRACK_FIVED, UFO_TRACK_PLAIN, UFO_TRACK_COMPACT = 1, 2, 4, 8
 
 _lib = None
 _lock = threading.Lock()

@@ -65,6 +65,7 @@ F_WEAKZ = 1 << 11       # teapot: weak term structurally zero (poison-only)
 F_YOSHIDA = 1 << 12     # teapot: 4th-order Yoshida splitting instead of TEAPOT
 F_CIRCLE = 1 << 13      # aperture: x*x + y*y < c (table: [c])
 F_SPLITO = 1 << 14      # teapot: exit outer drift is its own constant, after the others
+F_PSER = 1 << 15        # kick/teapot (FMA programs): dense power series appended last
 # drift form of teapot outer/inner drifts packed in bits 16..19
 SH_FOUTER, SH_FINNER = 16, 18
 
@@ -234,14 +235,14 @@ class KickSpec:
         return not ((nn == 2 and mn == 2) or (nn == 3 and mn == 4) or mn == 0)
 
     def flops_fast(self):
-        """FMA-mode operations per kick.  General kicks are one complex Horner
-        pass over power-series coefficients: per order below the top 2
-        coefficient scalings + 4 FMA (10 flops), 2 scalings for the top
-        coefficient, the strength factor and 2 FMA for the update."""
+        """FMA-mode FP64 flops the kernels execute per kick (an FMA counts 2).
+        General kicks are one complex Horner pass over the dense power series
+        prepared on the host (F_PSER): 4 FMA per order below the top one and 2
+        FMA for the update, the strength factor o being the particle's own."""
         if self.general():
             _, _, mn, ms, _ = self.packed()
             top = (mn | ms).bit_length() - 1
-            return 10 * top + 2 + (0 if self.achro else 1) + 4
+            return 8 * top + 4
         total = 0
         for lst, skew in ((self.norm, False), (self.skew, True)):
             total += _horner_flops(lst, self.achro, skew, fast=True)
@@ -419,8 +420,19 @@ class _Lowerer:
         dflops_i = 11 if exact else {DF_MUL: 4, DF_MUL2: 6, DF_DIV: 6}[fi]
         wflops = 2 if fl & F_WEAK else 0
         op.flops = 2 * dflops_o + (slices - 1) * dflops_i + slices * (ks.flops() + wflops)
-        fd = 11 if exact else 4
-        op.flops_fast = (slices + 1) * fd + slices * (ks.flops_fast() + wflops)
+        if exact:
+            op.flops_fast = (slices + 1) * 11 + slices * (ks.flops_fast() + wflops)
+        else:
+            # what the FMA-mode kernel executes (csrc/ops.cuh: teapot_v): drifts 2
+            # FMA each; the kick strength formed once per element (quadrupole
+            # t = K o: 1 mul; sextupole t = (K o) 0.5 and 2t: 3 operations); per
+            # slice the kick (quadrupole 2 FMA, sextupole 2 mul + 3 FMA, general
+            # the power-series Horner) and the weak term (1 FMA)
+            pat = 0 if nsk else 1 if (nn == 2 and mn == 2) else 2 if (nn == 3 and mn == 4) \
+                else 3 if mn == 0 else 0
+            per_elem = {0: 0, 1: 1, 2: 3, 3: 0}[pat]
+            kick = {0: ks.flops_fast() if (mn | ms) else 0, 1: 4, 2: 8, 3: 0}[pat]
+            op.flops_fast = 4 * (slices + 1) + per_elem + slices * (kick + wflops)
         self.emit(op)
 
     def _yoshida(self, Lf, slices, ks, weak, elem):
@@ -452,7 +464,11 @@ class _Lowerer:
         achro = bool(self.flags & ACHROMATIC)
         per_elem = {0: 0, 1: 3 + (0 if achro else 1), 2: 4 + (0 if achro else 1), 3: 0}[pat] + \
             (3 if wc else 0)
-        kick = {0: ks.flops() + 4, 1: 4, 2: 10, 3: 0}[pat]
+        # general kicks: FMA programs evaluate the dense power series (plus the
+        # strength factor o w), strict ones the reference's Horner + the
+        # weighted accumulation
+        general = ks.flops_fast() + 1 if self.flags & FMA else ks.flops() + 4
+        kick = {0: general, 1: 4, 2: 10, 3: 0}[pat]
         op.flops = op.flops_fast = per_elem + slices * (16 + 3 * (kick + (2 if wc else 0)))
         self.emit(op)
 
@@ -962,8 +978,9 @@ def _merge_drifts(ops):
     commutes with the alignment shifts between it and the teapot (they move x
     and y, not px and py), so those may lie in between; apertures, edges and
     observation points may not.  A teapot that absorbs a drift after it keeps
-    its exit length as a separate constant (F_SPLITO).  Flop counts keep the
-    merged drifts (the algorithmic count is the reference's)."""
+    its exit length as a separate constant (F_SPLITO).  The reference count
+    (``flops``) keeps the merged drifts; the executed count (``flops_fast``)
+    does not: their arithmetic is gone."""
     def teapot_ok(op):
         return (op.kind == OP_TEAPOT and not op.flags & (F_EXACT | F_YOSHIDA)
                 and (op.flags >> SH_FOUTER) & 3 == DF_MUL)
@@ -990,7 +1007,6 @@ def _merge_drifts(ops):
                 split(t)
                 t.consts[0] = op.consts[0] + t.consts[0]
                 t.flops += op.flops
-                t.flops_fast += op.flops_fast
                 i += 1
                 continue
             k = len(out) - 1
@@ -1001,12 +1017,60 @@ def _merge_drifts(ops):
                 split(t)
                 t.consts[-1] = t.consts[-1] + op.consts[0]
                 t.flops += op.flops
-                t.flops_fast += op.flops_fast
                 i += 1
                 continue
         out.append(op)
         i += 1
     return out
+
+
+def _rcp_factorials(n):
+    """1/k! for k = 0..n-1, each RN(1 / RN(k!)) with k! built by successive
+    multiplication: the same doubles as the kernels' constant table
+    (csrc/ufo_gb300.cu: ensure_constants)."""
+    out, fact = [], 1.0
+    for k in range(n):
+        if k > 0:
+            fact *= float(k)
+        out.append(1.0 / fact)
+    return out
+
+
+def _append_series(ops):
+    """FMA programs: a general kick (not the quadrupole or sextupole short
+    form) is one complex Horner pass over S(z) = sum_n (kn_n + i ks_n) z^n / n!.
+    Append to each such op, after all its other constants, the dense power
+    series a_n = RN(kn_n * RN(1/n!)), b_n likewise, n = 0..top (structurally
+    zero terms +0.0): the products the kernels would otherwise form at every
+    order of every slice, with the same rounding, so results are unchanged
+    bit for bit (F_PSER)."""
+    for op in ops:
+        if op.kind not in (OP_KICK, OP_TEAPOT) or op.flags & F_EXACT:
+            continue
+        if op.kind == OP_KICK:
+            nn, ns, mn, ms = op.ints[:4]
+            first = 0
+        else:
+            nn, ns, mn, ms = op.ints[1:5]
+            if op.flags & F_YOSHIDA:
+                first = 7
+            else:
+                fi = (op.flags >> SH_FINNER) & 3
+                first = 1 + (0 if op.ints[0] <= 1 else 4 if fi == DF_DIV else 1)
+        general = bool(ms) or not ((nn == 2 and mn == 2) or (nn == 3 and mn == 4) or mn == 0)
+        if not general or not (mn | ms):
+            continue
+        M = (mn | ms).bit_length()
+        rf = _rcp_factorials(M)
+        cn = op.consts[first:first + bin(mn).count('1')]
+        cs = op.consts[first + len(cn):first + len(cn) + bin(ms).count('1')]
+        a, b = [], []
+        for lst, mask, out in ((cn, mn, a), (cs, ms, b)):
+            it = iter(lst)
+            for j in range(M):
+                out.append(next(it) * rf[j] if mask >> j & 1 else Val.of(0.0))
+        op.consts = op.consts + a + b
+        op.flags |= F_PSER
 
 
 def compile_line(line, flags=0, parameters=(), where=(), seed_values=None, count=None,
@@ -1037,6 +1101,8 @@ def compile_line(line, flags=0, parameters=(), where=(), seed_values=None, count
         lower_element(lw, elem, idx, prm, per[idx], binds[idx], seed_values, coord_cols)
     if flags & FMA:
         lw.segments = [_merge_drifts(seg) for seg in lw.segments]
+        for seg in lw.segments:
+            _append_series(seg)
     if dump_end is None:
         dump_end = -1 in where
     if count is None:

@@ -1,8 +1,9 @@
 // diff.cu -- tangent map and hand-written adjoint of the one-turn map.
 //
 // Differentiation runs on its own opcode list (built by ufo_gb300/diff.py from
-// the compiled line): drifts, teapot elements, thin kicks, alignments and
-// constant edges.  Every kick of the reference (ufo/methods.py:45-76, the
+// the compiled line): drifts, teapot elements, thin kicks, alignments, edges
+// (with a fringe angle that may depend on dp) and the exact thick quadrupole
+// and sector-bend maps.  Every kick of the reference (ufo/methods.py:45-76, the
 // Horner scheme) is the complex polynomial
 //     S(z) = o * sum_n (a_n + i b_n) z^n,   z = x + i y,
 //     a_n = kn_n / n!,  b_n = ks_n / n!,
@@ -37,8 +38,11 @@
 
 namespace ufo_diff {
 
-enum : int { D_NOP = 0, D_DRIFT, D_TEAPOT, D_KICK, D_ALIGN, D_EDGE };
+enum : int { D_NOP = 0, D_DRIFT, D_TEAPOT, D_KICK, D_ALIGN, D_EDGE, D_THICK };
 constexpr int KHDR = 6;   // kick constants: Lo, Li, W, g0, g1, Lx (exit), then a[M], b[M]
+constexpr int DT_BEND = 1;      // D_THICK flag: sector bend (h^2 focusing, dispersion term)
+constexpr int DE_RTPSI = 1;     // D_EDGE flag: fringe angle psi depends on the job's dp
+constexpr int THICK_SLOTS = 2;  // tape slots of a thick element per turn
 
 struct DOp {
   int kind, flags, toff, N, M, pslot, pm, achro;
@@ -135,6 +139,122 @@ __device__ __forceinline__ void fwd_kick(St &s, const double *a, int M, double o
   s.py = fma(o, si, s.py);
 }
 
+// The exact thick maps (ufo/methods.py:99-134 quadrupole, :136-196 sector
+// bend) per plane: q' = C q + Sw pq + disp D1, pq' = -K Sw q + C pq + disp Sw,
+// with the plane's focusing strength K (q'' = -K q; K_x = o (k1 + h^2),
+// K_y = -o k1, o = 1 when achromatic), C = cos(sqrt(K) L) (cosh for K < 0),
+// Sw = sin(sqrt(K) L) / sqrt(K) (sinh), D1 = (1 - C) / K, and the bend's
+// horizontal dispersion disp = dp h o.  Power series in u = K L^2 for
+// |u| < 1 (no cancellation near K = 0), closed forms above; the derivatives
+// in K are dC = -L Sw / 2, dSw = (L C - Sw) / (2K), dD1 = (L Sw / 2 - D1) / K.
+// Same arithmetic as ufo_gb300/diff.py: thick_functions.
+template <bool DERIV>
+__device__ __forceinline__ void thick_fns(double K, double L, double &C, double &Sw, double &D1,
+                                          double &dC, double &dSw, double &dD1) {
+  const double u = K * L * L;
+  if (fabs(u) < 1.0) {
+    // Horner over n = 13..0 of (-u)^n / (2n)!, / (2n+1)!, / (2n+2)! (and
+    // n (-1)^n u^(n-1) / (2n+1)!, / (2n+2)! for the derivatives)
+    double c = 0.0, sw = 0.0, d1 = 0.0, ds = 0.0, dd = 0.0;
+    double f2n = 1.0;  // (2n)! for n = 13, built downwards from the top
+#pragma unroll
+    for (int k = 1; k <= 26; ++k) f2n *= k;
+#pragma unroll
+    for (int n = 13; n >= 0; --n) {
+      const double sg = (n & 1) ? -1.0 : 1.0;
+      const double i0 = sg / f2n;                              // 1/(2n)!
+      const double i1 = i0 / (2 * n + 1);                      // 1/(2n+1)!
+      const double i2 = i1 / (2 * n + 2);                      // 1/(2n+2)!
+      c = fma(c, u, i0);
+      sw = fma(sw, u, i1);
+      d1 = fma(d1, u, i2);
+      if (DERIV && n >= 1) {
+        ds = fma(ds, u, n * i1);
+        dd = fma(dd, u, n * i2);
+      }
+      if (n > 0) f2n /= static_cast<double>((2 * n) * (2 * n - 1));
+    }
+    C = c;
+    Sw = L * sw;
+    D1 = L * L * d1;
+    if (DERIV) {
+      dSw = L * L * L * ds;
+      dD1 = L * L * L * L * dd;
+    }
+  } else {
+    const double w = sqrt(fabs(K));
+    if (K > 0) {
+      double sn, cs;
+      sincos(w * L, &sn, &cs);
+      C = cs;
+      Sw = sn / w;
+    } else {
+      C = cosh(w * L);
+      Sw = sinh(w * L) / w;
+    }
+    D1 = (1.0 - C) / K;
+    if (DERIV) {
+      dSw = (L * C - Sw) / (2.0 * K);
+      dD1 = (0.5 * L * Sw - D1) / K;
+    }
+  }
+  if (DERIV) dC = -0.5 * L * Sw;
+}
+
+// one plane of a thick element forward; with `tangent` the plane's two
+// tangent rows tq, tp (4 columns each) too
+__device__ __forceinline__ void thick_plane_fwd(double &q, double &pq, double *tq, double *tp,
+                                                double K, double L, double disp, bool tangent) {
+  double C, Sw, D1, dC, dSw, dD1;
+  thick_fns<false>(K, L, C, Sw, D1, dC, dSw, dD1);
+  const double A = -K * Sw;
+  const double q0 = q;
+  q = fma(C, q0, fma(Sw, pq, disp * D1));
+  pq = fma(A, q0, fma(C, pq, disp * Sw));
+  if (tangent)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const double t = tq[j];
+      tq[j] = fma(C, t, Sw * tp[j]);
+      tp[j] = fma(A, t, C * tp[j]);
+    }
+}
+
+// reverse of one plane of a thick element at the entry state (q, pq) and
+// entry tangent rows (tq, tp; tangent mode): cotangents (qb, pqb) and the
+// tangent-row cotangents (bq, bp) are mapped back through the transposed map;
+// returns the cotangent of the plane's focusing strength K
+__device__ __forceinline__ double thick_plane_rev(double &qb, double &pqb, double *bq, double *bp,
+                                                  const double *tq, const double *tp, double q,
+                                                  double pq, double K, double L, double disp,
+                                                  bool tangent) {
+  double C, Sw, D1, dC, dSw, dD1;
+  thick_fns<true>(K, L, C, Sw, D1, dC, dSw, dD1);
+  const double A = -K * Sw, dA = fma(-K, dSw, -Sw);
+  double Kb = fma(qb, fma(dC, q, fma(dSw, pq, disp * dD1)),
+                  pqb * fma(dA, q, fma(dC, pq, disp * dSw)));
+  if (tangent)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      Kb = fma(bq[j], fma(dC, tq[j], dSw * tp[j]), fma(bp[j], fma(dA, tq[j], dC * tp[j]), Kb));
+      const double b = bq[j];
+      bq[j] = fma(C, b, A * bp[j]);
+      bp[j] = fma(Sw, b, C * bp[j]);
+    }
+  const double b = qb;
+  qb = fma(C, b, A * pqb);
+  pqb = fma(Sw, b, C * pqb);
+  return Kb;
+}
+
+// tan of an edge's vertical angle: constant, or the fringe-field psi of the
+// job's curvature (psi = e - 2 curv fint' / cos(e) (1 + sin^2 e), SLAC-75)
+__device__ __forceinline__ double edge_t2(int flags, const double *c, double curv) {
+  if (flags & DE_RTPSI)
+    return tan(__ldg(c + 2) - 2.0 * curv * __ldg(c + 3) / __ldg(c + 4) * __ldg(c + 5));
+  return __ldg(c + 2);
+}
+
 // tape slot of field f of kick k in turn tt (counted from the start of the
 // group of segments being taped); rich-tape fields: x, y, Re S', Im S'.
 // Warp-blocked: one warp's values for one turn are a contiguous run (the
@@ -165,7 +285,7 @@ __device__ void turn_forward(St &s, const DiffArgs &a, const double *T0, double 
         s.y -= __ldg(c + 1);
         break;
       case D_EDGE: {
-        const double curv = __ldg(c) * oo, e1 = __ldg(c + 1), e2 = __ldg(c + 2);
+        const double curv = __ldg(c) * oo, e1 = __ldg(c + 1), e2 = edge_t2(op.flags, c, curv);
         const double x0 = s.x, y0 = s.y;
         s.px = fma(x0 * curv, e1, s.px);
         s.py = fma(-(y0 * curv), e2, s.py);
@@ -199,6 +319,29 @@ __device__ void turn_forward(St &s, const DiffArgs &a, const double *T0, double 
           if (tp && W != 0.0) fwd_weak(s, W, tangent);
           if (tp) fwd_drift(s, sl < N - 1 ? Li : Lx, tangent);
         }
+        break;
+      }
+      case D_THICK: {
+        const double L = __ldg(c), k1 = __ldg(c + 1), h = __ldg(c + 2);
+        const int k = kidx;
+        kidx += THICK_SLOTS;
+        if (tape) {  // entry state and tangent: x, y, T rows x, y | px, py, T rows px, py
+          double *t = a.tape;
+          t[tidx(a, tt, k, 0, nf, j)] = s.x;
+          t[tidx(a, tt, k, 1, nf, j)] = s.y;
+          t[tidx(a, tt, k + 1, 0, nf, j)] = s.px;
+          t[tidx(a, tt, k + 1, 1, nf, j)] = s.py;
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            t[tidx(a, tt, k, 2 + q, nf, j)] = s.T[q];
+            t[tidx(a, tt, k, 6 + q, nf, j)] = s.T[8 + q];
+            t[tidx(a, tt, k + 1, 2 + q, nf, j)] = s.T[4 + q];
+            t[tidx(a, tt, k + 1, 6 + q, nf, j)] = s.T[12 + q];
+          }
+        }
+        const double disp = (op.flags & DT_BEND) ? (1.0 / o - 1.0) * h * oo : 0.0;
+        thick_plane_fwd(s.x, s.px, s.T, s.T + 4, oo * fma(h, h, k1), L, disp, tangent);
+        thick_plane_fwd(s.y, s.py, s.T + 8, s.T + 12, -oo * k1, L, 0.0, tangent);
         break;
       }
       default:
@@ -305,7 +448,7 @@ __device__ void turn_reverse(Bar &b, const DiffArgs &a, const double *T0, double
       case D_ALIGN:
         break;  // translation: cotangents unchanged
       case D_EDGE: {
-        const double curv = __ldg(c) * oo, e1 = __ldg(c + 1), e2 = __ldg(c + 2);
+        const double curv = __ldg(c) * oo, e1 = __ldg(c + 1), e2 = edge_t2(op.flags, c, curv);
         b.x = fma(b.px * curv, e1, b.x);
         b.y = fma(-(b.py * curv), e2, b.y);
         if (tangent)
@@ -332,6 +475,34 @@ __device__ void turn_reverse(Bar &b, const DiffArgs &a, const double *T0, double
         if (op.pslot >= 0) {
           double &p = a.pbar[static_cast<int64_t>(op.pslot) * a.n_jobs + j];
           p = fma(g0, __ldg(c + 3), fma(g1, __ldg(c + 4), p));
+        }
+        break;
+      }
+      case D_THICK: {
+        const double L = __ldg(c), k1 = __ldg(c + 1), h = __ldg(c + 2);
+        kidx -= THICK_SLOTS;
+        const int nf = 10;
+        const double *t = a.tape;
+        double ex[4], epx[4], ey[4], epy[4];  // entry tangent rows
+        if (tangent)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            ex[q] = t[tidx(a, tt, kidx, 2 + q, nf, j)];
+            ey[q] = t[tidx(a, tt, kidx, 6 + q, nf, j)];
+            epx[q] = t[tidx(a, tt, kidx + 1, 2 + q, nf, j)];
+            epy[q] = t[tidx(a, tt, kidx + 1, 6 + q, nf, j)];
+          }
+        const double x = t[tidx(a, tt, kidx, 0, nf, j)], y = t[tidx(a, tt, kidx, 1, nf, j)];
+        const double px = t[tidx(a, tt, kidx + 1, 0, nf, j)];
+        const double py = t[tidx(a, tt, kidx + 1, 1, nf, j)];
+        const double disp = (op.flags & DT_BEND) ? (1.0 / o - 1.0) * h * oo : 0.0;
+        const double kbx = thick_plane_rev(b.x, b.px, b.T, b.T + 4, ex, epx, x, px,
+                                           oo * fma(h, h, k1), L, disp, tangent);
+        const double kby = thick_plane_rev(b.y, b.py, b.T + 8, b.T + 12, ey, epy, y, py, -oo * k1,
+                                           L, 0.0, tangent);
+        if (op.pslot >= 0) {  // dK_x/dk1 = o, dK_y/dk1 = -o
+          double &p = a.pbar[static_cast<int64_t>(op.pslot) * a.n_jobs + j];
+          p = fma(oo, kbx - kby, p);
         }
         break;
       }
@@ -553,7 +724,21 @@ __device__ void turn_forward_pair(Half &h, const DiffArgs &a, const double *T0, 
       case D_EDGE: {
         const double curv = __ldg(c) * oo;
         const double t = h.u * curv;
-        h.pu = fma(even ? t : -t, __ldg(c + (even ? 1 : 2)), h.pu);
+        h.pu = fma(even ? t : -t, even ? __ldg(c + 1) : edge_t2(op.flags, c, curv), h.pu);
+        break;
+      }
+      case D_THICK: {
+        const double L = __ldg(c), k1 = __ldg(c + 1), hh = __ldg(c + 2);
+        const int k = kidx;
+        kidx += THICK_SLOTS;
+        if (tape && write) {  // entry state: x, px by the even lane; y, py by the odd lane
+          double *t0 = a.tape + tidx(a, tt, k, 0, 4, j);
+          t0[even ? 0 : TLANES] = h.u;
+          t0[(even ? 2 : 3) * TLANES] = h.pu;
+        }
+        const double K = even ? oo * fma(hh, hh, k1) : -oo * k1;
+        const double disp = (even && (op.flags & DT_BEND)) ? (1.0 / o - 1.0) * hh * oo : 0.0;
+        thick_plane_fwd(h.u, h.pu, nullptr, nullptr, K, L, disp, false);
         break;
       }
       case D_KICK:
@@ -659,7 +844,25 @@ __device__ void turn_reverse_pair(Half &bh, const DiffArgs &a, const double *T0,
       case D_EDGE: {
         const double curv = __ldg(c) * oo;
         const double t = bh.pu * curv;
-        bh.u = fma(even ? t : -t, __ldg(c + (even ? 1 : 2)), bh.u);
+        bh.u = fma(even ? t : -t, even ? __ldg(c + 1) : edge_t2(op.flags, c, curv), bh.u);
+        break;
+      }
+      case D_THICK: {
+        const double L = __ldg(c), k1 = __ldg(c + 1), hh = __ldg(c + 2);
+        kidx -= THICK_SLOTS;
+        const int m = ((kidx + THICK_SLOTS - 1) / CHUNK) * CHUNK;  // a chunk start in range
+        if (write && even && m >= kidx && m >= 2 * CHUNK) prefetch_chunk(a, tt, m - 2 * CHUNK, j);
+        const double *t0 = a.tape + tidx(a, tt, kidx, 0, 4, j);
+        const double q = t0[even ? 0 : TLANES], pq = t0[(even ? 2 : 3) * TLANES];
+        const double K = even ? oo * fma(hh, hh, k1) : -oo * k1;
+        const double disp = (even && (op.flags & DT_BEND)) ? (1.0 / o - 1.0) * hh * oo : 0.0;
+        const double kb = thick_plane_rev(bh.u, bh.pu, nullptr, nullptr, nullptr, nullptr, q, pq,
+                                          K, L, disp, false);
+        const double kb_other = other(kb);  // every lane: the shuffle needs the whole warp
+        if (op.pslot >= 0 && write && even) {  // dK_x/dk1 = o, dK_y/dk1 = -o
+          double &p = a.pbar[static_cast<int64_t>(op.pslot) * a.n_jobs + j];
+          p = fma(oo, kb - kb_other, p);
+        }
         break;
       }
       case D_KICK:

@@ -23,7 +23,8 @@ enum : int { DF_MUL = 0, DF_MUL2 = 1, DF_DIV = 2 };
 enum : int {
   F_ACHRO = 1 << 0, F_EXACT = 1 << 1, F_WEAK = 1 << 2, F_RTPSI = 1 << 3, F_T1 = 1 << 4,
   F_T2 = 1 << 5, F_CONST = 1 << 6, F_AX = 1 << 7, F_AY = 1 << 8, F_T1Z = 1 << 9,
-  F_T2Z = 1 << 10, F_WEAKZ = 1 << 11, F_YOSHIDA = 1 << 12, F_CIRCLE = 1 << 13, F_SPLITO = 1 << 14
+  F_T2Z = 1 << 10, F_WEAKZ = 1 << 11, F_YOSHIDA = 1 << 12, F_CIRCLE = 1 << 13, F_SPLITO = 1 << 14,
+  F_PSER = 1 << 15
 };
 constexpr int SH_FOUTER = 16, SH_FINNER = 18;
 
@@ -332,6 +333,24 @@ __device__ __noinline__ PxPy kick_cplx_ool(double x, double y, double px, double
   return {fma_(-f, pr, px), fma_(f, pi, py)};
 }
 
+// The same kick from a dense power series prepared on the host (F_PSER:
+// a_n = RN(kn_n * RN(1/n!)), then b_n, n < M): the products poly_cplx forms at
+// every order are loaded instead, so the result is the same bit for bit with
+// 4 FMAs per order.
+__device__ __noinline__ PxPy kick_pser_ool(double x, double y, double px, double py, double f,
+                                           int M, const double *c) {
+  double pr = ld(c + M - 1), pi = ld(c + 2 * M - 1);
+  for (int n = M - 2; n >= 0; --n) {
+    const double tr = fma_(pr, x, fma_(-pi, y, ld(c + n)));
+    pi = fma_(pr, y, fma_(pi, x, ld(c + M + n)));
+    pr = tr;
+  }
+  return {fma_(-f, pr, px), fma_(f, pi, py)};
+}
+
+// terms of the dense series of a kick with masks mn, ms (highest order + 1)
+UFO_DEV int pser_len(uint32_t mn, uint32_t ms) { return 32 - __clz(mn | ms); }
+
 UFO_DEV void kick_cplx(State &s, uint32_t mn, uint32_t ms, const double *c, bool achro,
                        double w = 1.0) {
   const double f = mul(achro ? 1.0 : s.o, w);
@@ -481,7 +500,7 @@ __device__ __noinline__ PxPy slow_slice(double x, double y, double px, double py
 
 template <bool FMA, int PAT, bool WEAK>
 UFO_DEV void tp_slice(State &s, int nn, int ns, uint32_t mn, uint32_t ms, const double *ck,
-                      bool achro, double t, double t2, double W) {
+                      bool achro, double t, double t2, double W, const double *ps = nullptr) {
   if (s.bad_o || nf(s.x) || nf(s.y)) {
     const PxPy r = slow_slice<FMA>(s.x, s.y, s.px, s.py, s.o, s.bad_o, nn, ns, mn, ms, ck, achro,
                                    WEAK, W);
@@ -490,7 +509,11 @@ UFO_DEV void tp_slice(State &s, int nn, int ns, uint32_t mn, uint32_t ms, const 
     return;
   }
   if (PAT == 0) {
-    if (FMA && (mn | ms) != 0u) {
+    if (FMA && ps) {  // t: the strength factor o (1 when achromatic)
+      const PxPy r = kick_pser_ool(s.x, s.y, s.px, s.py, t, pser_len(mn, ms), ps);
+      s.px = r.px;
+      s.py = r.py;
+    } else if (FMA && (mn | ms) != 0u) {
       kick_cplx(s, mn, ms, ck, achro);
     } else {
       const PxPy r = kick_ool<FMA>(s.x, s.y, s.px, s.py, s.o, s.bad_o, nn, ns, mn, ms, ck, achro,
@@ -532,16 +555,22 @@ UFO_DEV void teapot_v(State &s, const Op &op, const double *c) {
   if (PAT == 1) t = mul(ld(ck), o1);
   if (PAT == 2) t = mul(mul(ld(ck), o1), 0.5);
   if (FMA && PAT == 2) t2 = add(t, t);
+  // general kicks of FMA programs: the dense series after every other constant
+  const double *ps = nullptr;
+  if (FMA && PAT == 0 && (op.flags & F_PSER)) {
+    ps = ck + __popc(mn) + __popc(ms) + (WEAK ? 1 : 0) + ((op.flags & F_SPLITO) ? 1 : 0);
+    t = o1;
+  }
   const double Li = DIVIN ? 0.0 : ld(ci);
   drift_L<FMA>(s, Lo);
   for (int sl = 1; sl < N; ++sl) {
-    tp_slice<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, t, t2, W);
+    tp_slice<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, t, t2, W, ps);
     if (DIVIN)
       drift_div<FMA>(s, ci);
     else
       drift_L<FMA>(s, Li);
   }
-  tp_slice<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, t, t2, W);
+  tp_slice<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, t, t2, W, ps);
   // exit outer drift: its own constant after the others when a following
   // drift was merged into it (FMA programs)
   double Lx = Lo;
@@ -560,8 +589,14 @@ UFO_DEV void teapot_v(State &s, const Op &op, const double *c) {
 // strengths of the quadrupole/sextupole patterns are formed once per element.
 template <bool FMA, int PAT, bool WEAK>
 UFO_DEV void y_kick(State &s, int nn, int ns, uint32_t mn, uint32_t ms, const double *ck,
-                    bool achro, double w, double t, double t2, double Ww) {
-  if (PAT == 0 && FMA && (mn | ms) != 0u) {
+                    bool achro, double w, double t, double t2, double Ww,
+                    const double *ps = nullptr) {
+  if (PAT == 0 && FMA && ps) {
+    const PxPy r = kick_pser_ool(s.x, s.y, s.px, s.py, mul(achro ? 1.0 : s.o, w),
+                                 pser_len(mn, ms), ps);
+    s.px = r.px;
+    s.py = r.py;
+  } else if (PAT == 0 && FMA && (mn | ms) != 0u) {
     kick_cplx(s, mn, ms, ck, achro, w);
   } else if (PAT == 0) {
     // unweighted kick from zero momenta: r = (-dpx, +dpy)
@@ -621,13 +656,16 @@ UFO_DEV void yoshida_v(State &s, const Op &op, const double *c) {
     W1 = mul(W, w1);
     W2 = mul(W, w2);
   }
+  const double *ps = (FMA && PAT == 0 && (op.flags & F_PSER))
+                         ? ck + __popc(mn) + __popc(ms) + (WEAK ? 1 : 0)
+                         : nullptr;
   for (int sl = 0; sl < N; ++sl) {
     drift_L<FMA>(s, d0);
-    y_kick<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, w0, t0, u0, W0);
+    y_kick<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, w0, t0, u0, W0, ps);
     drift_L<FMA>(s, d1);
-    y_kick<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, w1, t1, u1, W1);
+    y_kick<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, w1, t1, u1, W1, ps);
     drift_L<FMA>(s, d2);
-    y_kick<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, w2, t2, u2, W2);
+    y_kick<FMA, PAT, WEAK>(s, nn, ns, mn, ms, ck, achro, w2, t2, u2, W2, ps);
     drift_L<FMA>(s, d3);
   }
 }

@@ -109,6 +109,14 @@ UFO_DEV void one_turn(State &s, const TrackArgs &a, const double *tab, int64_t p
         break;
       case OP_KICK: {
         const bool bad = s.bad_o || nf(s.x) || nf(s.y);
+        if (FMA && !bad && (op.flags & F_PSER)) {  // dense series after the coefficients
+          const uint32_t mn = static_cast<uint32_t>(op.i2), ms = static_cast<uint32_t>(op.i3);
+          const PxPy r = kick_pser_ool(s.x, s.y, s.px, s.py, (op.flags & F_ACHRO) ? 1.0 : s.o,
+                                       pser_len(mn, ms), c + __popc(mn) + __popc(ms));
+          s.px = r.px;
+          s.py = r.py;
+          break;
+        }
         const PxPy r = kick_ool<FMA>(s.x, s.y, s.px, s.py, s.o, s.bad_o, op.i0, op.i1,
                                      static_cast<uint32_t>(op.i2), static_cast<uint32_t>(op.i3),
                                      c, op.flags & F_ACHRO, bad);
@@ -216,6 +224,142 @@ __global__ void __launch_bounds__(32) track_kernel(TrackArgs a) {
       continue;  // re-check: a lane that got a zero-turn particle needs another
     }
     if (__all_sync(ALL, p < 0)) break;
+    if (p >= 0) {
+      one_turn<FMA, FULL>(s, a, tab, p);
+      const bool lost = is_lost(s, a.mode);
+      if (!lost) ++s.turn;
+      if (lost || s.turn >= target) {
+        store_final(s, a, p);
+        p = -1;
+      }
+    }
+  }
+}
+
+// ------------------------------------------------- CTA-compacting variant
+// The same persistent loop with many warps per CTA, and one more step once
+// the work counter is exhausted: at every turn boundary the CTA packs its
+// surviving particles into its lowest warps through shared memory (a ballot
+// + popc rank within each warp, a prefix over the warps), so the survivors of
+// an uneven scan keep filling whole warps instead of thinning out across all
+// of them.  Moving a particle between lanes is a copy of its state: every
+// particle's arithmetic, and so every result bit, is the one of the other
+// kernels.
+// Phase A (work left in the counter): each warp refills its own lanes, no
+// barrier, exactly as track_kernel.  A warp that finds the counter exhausted
+// (itself, or through the CTA's flag another warp set) enters phase B, where
+// the CTA meets at one barrier per turn: every warp reaches phase B (the flag
+// is set once and only read afterwards), so every barrier is reached by the
+// whole CTA.  Emptied warps stay in the loop (they take part in the barriers
+// and issue no FP64 work) until the CTA has no particle left.
+struct Parked {        // a particle in flight, moved between lanes
+  double x, px, y, py, z, dp;
+  int64_t p;
+  int turn, target;
+  int seed;
+  int pad;
+};
+
+constexpr int CTA_MAX_WARPS = 16;
+
+template <bool FMA, bool FULL>
+__global__ void __launch_bounds__(CTA_MAX_WARPS * 32, 1) track_kernel_cta(TrackArgs a) {
+  extern __shared__ Parked parked[];  // one slot per thread of the CTA
+  // lanes with a particle per warp, double-buffered by barrier phase (a warp
+  // one phase ahead writes the other buffer)
+  __shared__ int warp_active[2][CTA_MAX_WARPS];
+  __shared__ int exhausted_flag;  // set once the work counter is exhausted
+  const unsigned ALL = 0xffffffffu;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwarps = blockDim.x >> 5;
+  const unsigned lt_mask = (1u << lane) - 1u;
+  volatile int *flag = &exhausted_flag;
+  if (threadIdx.x == 0) *flag = 0;
+  __syncthreads();
+  int64_t p = -1;
+  int sd = 0;
+  State s{};
+  int target = 0;
+  const double *tab = a.table;
+  // ---- phase A: refill from the counter, no barrier
+  bool exhausted = false;
+  while (true) {
+    if (*flag) exhausted = true;  // another warp found the counter exhausted
+    while (!exhausted) {
+      const unsigned need = __ballot_sync(ALL, p < 0);
+      if (!need) break;
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(a.queue, static_cast<unsigned long long>(__popc(need)));
+      base = __shfl_sync(ALL, base, leader);
+      if (base + __popc(need) > static_cast<unsigned long long>(a.n)) {
+        exhausted = true;
+        if (lane == leader) *flag = 1;  // the counter only grows: final
+      }
+      if (p < 0) {
+        const int64_t q = static_cast<int64_t>(base) + __popc(need & lt_mask);
+        if (q < a.n) {
+          p = q;
+          load_particle(s, a, p);
+          target = a.pturns ? a.pturns[p] : a.turns;
+          sd = a.seed ? a.seed[p] : 0;
+          tab = a.table + static_cast<int64_t>(sd) * a.stride;
+          if (sd < 0 || sd >= a.n_seeds) {  // seed outside the table: not tracked
+            if (a.lost) a.lost[p] = 0xffffffffu;
+            p = -1;
+          } else if (target <= 0) {  // nothing to track
+            store_final(s, a, p);
+            p = -1;
+          }
+        }
+      }
+    }
+    if (exhausted) break;  // warp-uniform
+    if (p >= 0) {  // a lane's particle needs no refill this turn
+      one_turn<FMA, FULL>(s, a, tab, p);
+      const bool lost = is_lost(s, a.mode);
+      if (!lost) ++s.turn;
+      if (lost || s.turn >= target) {
+        store_final(s, a, p);
+        p = -1;
+      }
+    }
+  }
+  // ---- phase B: one barrier per turn, survivors packed into the lowest warps
+  for (int k = 0;; ++k) {
+    const unsigned act = __ballot_sync(ALL, p >= 0);
+    if (lane == 0) warp_active[k & 1][warp] = __popc(act);
+    __syncthreads();
+    int total = 0, busy = 0, before = 0;
+    for (int w = 0; w < nwarps; ++w) {
+      const int c = warp_active[k & 1][w];
+      if (w < warp) before += c;
+      total += c;
+      busy += c > 0;
+    }
+    if (total == 0) break;  // CTA-uniform: every thread read the same counts
+    if ((total + 31) / 32 < busy) {  // CTA-uniform: packing frees a warp
+      if (p >= 0) {
+        Parked &d = parked[before + __popc(act & lt_mask)];
+        d.x = s.x; d.px = s.px; d.y = s.y; d.py = s.py; d.z = s.z; d.dp = s.dp;
+        d.p = p; d.turn = s.turn; d.target = target; d.seed = sd;
+      }
+      __syncthreads();
+      p = -1;
+      if (static_cast<int>(threadIdx.x) < total) {
+        const Parked &d = parked[threadIdx.x];
+        s.x = d.x; s.px = d.px; s.y = d.y; s.py = d.py; s.z = d.z; s.dp = d.dp;
+        s.o = dvd(1., add(s.dp, 1.));  // as load_particle: the same bits
+        s.opdp = add(1., s.dp);
+        s.bad_o = nf(s.o);
+        s.turn = d.turn;
+        p = d.p;
+        target = d.target;
+        sd = d.seed;
+        tab = a.table + static_cast<int64_t>(sd) * a.stride;
+      }
+      // the slots are rewritten only after the next phase's barrier
+    }
     if (p >= 0) {
       one_turn<FMA, FULL>(s, a, tab, p);
       const bool lost = is_lost(s, a.mode);
@@ -481,6 +625,15 @@ bool mask_fits(int n, int32_t mask) {
   return n == 32 || (m >> n) == 0u;
 }
 
+// constants of the dense power series of a general kick (F_PSER): 2 per
+// order up to the highest coefficient; -1 if the flag is set without one
+int64_t pser_consts(int flags, int32_t mn, int32_t ms) {
+  if (!(flags & ufo::F_PSER)) return 0;
+  const uint32_t m = static_cast<uint32_t>(mn) | static_cast<uint32_t>(ms);
+  if (m == 0u) return -1;
+  return 2 * static_cast<int64_t>(32 - __builtin_clz(m));
+}
+
 int drift_consts(int form, bool exact) {
   if (exact) return 1;
   return form == ufo::DF_MUL ? 1 : form == ufo::DF_MUL2 ? 2 : form == ufo::DF_DIV ? 4 : -1;
@@ -498,20 +651,26 @@ int64_t op_consts(const int32_t *w) {
       return 0;
     case ufo::OP_DRIFT:
       return drift_consts(w[3], exact);
-    case ufo::OP_KICK:
+    case ufo::OP_KICK: {
       if (!mask_fits(w[3], w[5]) || !mask_fits(w[4], w[6])) return -1;
-      return popc32(w[5]) + popc32(w[6]);
+      const int64_t ps = pser_consts(flags, w[5], w[6]);
+      if (ps < 0) return -1;
+      return popc32(w[5]) + popc32(w[6]) + ps;
+    }
     case ufo::OP_TEAPOT: {
-      if (flags & ufo::F_YOSHIDA) {  // [4 drifts][3 weights][kick][W]
+      const int64_t ps = pser_consts(flags, w[6], w[7]);
+      if (ps < 0) return -1;
+      if (flags & ufo::F_YOSHIDA) {  // [4 drifts][3 weights][kick][W][series]
         if (exact || w[3] < 1 || !mask_fits(w[4], w[6]) || !mask_fits(w[5], w[7])) return -1;
-        return 7 + popc32(w[6]) + popc32(w[7]) + ((flags & ufo::F_WEAK) ? 1 : 0);
+        return 7 + popc32(w[6]) + popc32(w[7]) + ((flags & ufo::F_WEAK) ? 1 : 0) + ps;
       }
       if (w[3] < 1 || !mask_fits(w[4], w[6]) || !mask_fits(w[5], w[7])) return -1;
+      if ((flags & ufo::F_PSER) && exact) return -1;
       const int fo = (flags >> ufo::SH_FOUTER) & 3, fi = (flags >> ufo::SH_FINNER) & 3;
       const int co = drift_consts(fo, exact), ci = w[3] > 1 ? drift_consts(fi, exact) : 0;
       if (co < 0 || ci < 0) return -1;
       return co + ci + popc32(w[6]) + popc32(w[7]) + ((flags & ufo::F_WEAK) ? 1 : 0) +
-             ((flags & ufo::F_SPLITO) ? 1 : 0);
+             ((flags & ufo::F_SPLITO) ? 1 : 0) + ps;
     }
     case ufo::OP_ALIGN:
       return 2;
@@ -631,6 +790,23 @@ int launch_kernels(ufo::TrackArgs &a, bool full, int sm_count, int warps_per_sm,
     else
       full ? ufo::track_plain_kernel<false, true><<<blocks, 128, 0, stream>>>(a)
            : ufo::track_plain_kernel<false, false><<<blocks, 128, 0, stream>>>(a);
+  } else if (a.flags & UFO_TRACK_COMPACT) {
+    UFO_CUDA(cudaMemsetAsync(a.queue, 0, sizeof(unsigned long long), stream));
+    // one CTA per SM (as many SMs as the particles' warps allow) of up to
+    // warps_per_sm warps (at most 16); survivors are packed within each CTA
+    const int64_t warps = (a.n + 31) / 32;
+    const int64_t ctas = warps < sm_count ? warps : sm_count;
+    int wpc = warps_per_sm < 1 ? 1 : warps_per_sm > ufo::CTA_MAX_WARPS ? ufo::CTA_MAX_WARPS
+                                                                          : warps_per_sm;
+    if (ctas * wpc > warps) wpc = static_cast<int>((warps + ctas - 1) / ctas);
+    const unsigned g = static_cast<unsigned>(ctas), tpb = static_cast<unsigned>(wpc * 32);
+    const size_t smem = sizeof(ufo::Parked) * tpb;
+    if (fma)
+      full ? ufo::track_kernel_cta<true, true><<<g, tpb, smem, stream>>>(a)
+           : ufo::track_kernel_cta<true, false><<<g, tpb, smem, stream>>>(a);
+    else
+      full ? ufo::track_kernel_cta<false, true><<<g, tpb, smem, stream>>>(a)
+           : ufo::track_kernel_cta<false, false><<<g, tpb, smem, stream>>>(a);
   } else {
     UFO_CUDA(cudaMemsetAsync(a.queue, 0, sizeof(unsigned long long), stream));
     // one warp per block so the block scheduler spreads warps evenly over the

@@ -29,8 +29,60 @@ import numpy as np
 from . import compiler as C
 from .flags import FMA
 
-D_NOP, D_DRIFT, D_TEAPOT, D_KICK, D_ALIGN, D_EDGE = range(6)
+D_NOP, D_DRIFT, D_TEAPOT, D_KICK, D_ALIGN, D_EDGE, D_THICK = range(7)
 KHDR = 6  # kick constants: Lo (entry), Li, W, dK/dk/pm!, dK/dk/(pm-1)!, Lx (exit), then a, b
+DT_BEND = 1  # D_THICK flag: sector bend (weak focusing h^2 and the dispersion term)
+DE_RTPSI = 1  # D_EDGE flag: fringe-field angle psi depends on the job's dp
+# tape slots a thick element takes per turn (tangent mode stores the entry
+# state and all 16 tangent entries: two slots of 10 fields)
+THICK_SLOTS = 2
+
+
+def thick_functions(K, L):
+    """The thick-map functions of the focusing strength K (q'' = -K q) over a
+    length L, for either sign of K, and their derivatives in K:
+        C = cos(sqrt(K) L) (cosh for K < 0), Sw = sin(sqrt(K) L)/sqrt(K)
+        (sinh(sqrt(-K) L)/sqrt(-K)), D1 = (1 - C)/K (the bend's dispersion
+        function); dC = -L Sw/2, dSw = (L C - Sw)/(2K), dD1 = (L Sw/2 - D1)/K.
+    Power series in u = K L^2 for |u| < 1 (no cancellation near K = 0),
+    closed forms above.  Arrays broadcast.  The same arithmetic as the
+    device code (csrc/diff.cu: thick_fns)."""
+    K = np.asarray(K, np.float64)
+    L = np.asarray(L, np.float64)
+    u = K * L * L
+    small = np.abs(u) < 1.0
+    # series: sum over n of (-u)^n / (2n)!, /(2n+1)!, /(2n+2)!; derivative
+    # series n (-1)^n u^(n-1) / (2n+1)! and / (2n+2)!
+    c = np.zeros_like(u)
+    sw = np.zeros_like(u)
+    d1 = np.zeros_like(u)
+    dsw = np.zeros_like(u)
+    dd1 = np.zeros_like(u)
+    us = np.where(small, u, 0.0)
+    for n in range(13, -1, -1):
+        sg = -1.0 if n % 2 else 1.0
+        c = c * us + sg / math.factorial(2 * n)
+        sw = sw * us + sg / math.factorial(2 * n + 1)
+        d1 = d1 * us + sg / math.factorial(2 * n + 2)
+        if n >= 1:
+            dsw = dsw * us + sg * n / math.factorial(2 * n + 1)
+            dd1 = dd1 * us + sg * n / math.factorial(2 * n + 2)
+    C_s, Sw_s, D1_s = c, L * sw, L * L * d1
+    dSw_s, dD1_s = L ** 3 * dsw, L ** 4 * dd1
+    with np.errstate(invalid='ignore', divide='ignore'):
+        w = np.sqrt(np.abs(K))
+        foc = K > 0
+        C_c = np.where(foc, np.cos(w * L), np.cosh(w * L))
+        Sw_c = np.where(foc, np.sin(w * L), np.sinh(w * L)) / w
+        D1_c = (1.0 - C_c) / K
+        dSw_c = (L * C_c - Sw_c) / (2 * K)
+        dD1_c = (0.5 * L * Sw_c - D1_c) / K
+    C = np.where(small, C_s, C_c)
+    Sw = np.where(small, Sw_s, Sw_c)
+    D1 = np.where(small, D1_s, D1_c)
+    dSw = np.where(small, dSw_s, dSw_c)
+    dD1 = np.where(small, dD1_s, dD1_c)
+    return C, Sw, D1, -0.5 * L * Sw, dSw, dD1
 
 
 def _torch():
@@ -97,7 +149,8 @@ class DiffProgram:
                 cols += hdr + list(range(off + h, off + h + Mt)) + \
                     list(range(off + h + M, off + h + M + Mt))
             else:
-                n = {D_DRIFT: 1, D_ALIGN: 2, D_EDGE: 3}.get(kind, 0)
+                n = {D_DRIFT: 1, D_ALIGN: 2, D_EDGE: 6 if op[1] & DE_RTPSI else 3,
+                     D_THICK: 3}.get(kind, 0)
                 cols += list(range(off, off + n))
             out_ops.append(op)
         cols.append(tab.shape[1] - 1)
@@ -131,9 +184,14 @@ class DiffProgram:
                 tab += [c(0) if fl & C.F_AX else 0.0, c(1) if fl & C.F_AY else 0.0]
             elif kind == C.OP_EDGE:
                 if fl & C.F_RTPSI:
-                    raise NotImplementedError('fringe-field edges with chromatic psi')
-                ops.append([D_EDGE, 0, len(tab), 0, 0, -1, 0, achro])
-                tab += [c(0), c(1) if fl & C.F_T1 else 0.0, c(2) if fl & C.F_T2 else 0.0]
+                    # fringe field with a chromatic angle: tan(psi) per job,
+                    # psi = e - 2 (A o) fint' / cos(e) (1 + sin^2 e) (SLAC-75;
+                    # ufo/methods.py:199-211)
+                    ops.append([D_EDGE, DE_RTPSI, len(tab), 0, 0, -1, 0, achro])
+                    tab += [c(0), c(1) if fl & C.F_T1 else 0.0, c(2), c(3), c(4), c(5)]
+                else:
+                    ops.append([D_EDGE, 0, len(tab), 0, 0, -1, 0, achro])
+                    tab += [c(0), c(1) if fl & C.F_T1 else 0.0, c(2) if fl & C.F_T2 else 0.0]
             elif kind in (C.OP_TEAPOT, C.OP_KICK):
                 if fl & C.F_YOSHIDA:
                     raise NotImplementedError('Yoshida elements are not differentiated')
@@ -184,6 +242,20 @@ class DiffProgram:
                 ops.append([D_TEAPOT if tp else D_KICK, 0, len(tab), N, M, ps, pm, achro])
                 tab += [Lo, Li, W, g0, g1, Lx] + cr + ci
                 kicks += N
+            elif kind in (C.OP_THICKQ, C.OP_THICKB):
+                # the exact thick maps (ufo/methods.py:99-134, :136-196): per
+                # plane q' = C q + Sw pq (+ dispersion), pq' = -K Sw q + C pq
+                # with K_x = o (k1 + h^2), K_y = -o k1 (o = 1 when ACHROMATIC)
+                if kind == C.OP_THICKQ:
+                    k1, L, h, fl_d = c(0), c(1), 0.0, 0
+                else:
+                    h, k1, L, fl_d = c(0), c(1), c(2), DT_BEND
+                ps, pm = slot.get(elem, (-1, 0))
+                if pm != 1:  # thick maps read k1 only
+                    ps = -1
+                ops.append([D_THICK, fl_d, len(tab), 0, 0, ps, 1, achro])
+                tab += [L, k1, h]
+                kicks += THICK_SLOTS
             else:
                 raise NotImplementedError(f'{C.OP_NAMES[kind]} elements are not differentiated')
         S = T.shape[0]
@@ -357,7 +429,7 @@ class OpticsModel:
     element strengths named in ``parameters``; one or many rows of strengths
     (error seeds) at a time."""
 
-    def __init__(self, line, flags, parameters, h_dp=1e-5, device=0):
+    def __init__(self, line, flags, parameters, h_dp=1e-4, device=0):
         self.line = line
         self.flags = flags
         self.parameters = list(parameters)

@@ -235,27 +235,45 @@ class StableAperture:
         return self._c.prog
 
     def _uses_turn(self):
-        import re
-        return any(type(e).__name__ == 'Aperture' and re.search(r'\bturn\b', str(e.window))
-                   for e in self._line.flatten())
+        """An aperture window or a time-dependent element reads ``turn``: the
+        particles' turn numbers must then not restart."""
+        return C.reads_turn(self._c.prog)
+
+    # resident warps per SM of the compacting kernel for a scan: measured
+    # best on the 196,608-particle dynamic-aperture grid (8 beat 12 and 16)
+    COMPACT_WARPS_PER_SM = 8
 
     def run(self, threads=1, compact=None):
-        """``compact`` (default: for 512+ turns and 16,384+ particles): track
-        the first turns/8 with the full persistent grid, then continue only the
-        survivors with a grid sized to them (resident warps per SM about
-        survivors / (0.9 x 32 x SMs)), so that the long-lived particles fill
-        whole warps; loss turns and coordinates are those of one run.  Not
-        used when an aperture window reads ``turn``."""
+        """One launch of the CTA-compacting persistent kernel (default,
+        ``compact=None`` or ``True``): once every particle has been handed out,
+        each CTA packs its survivors into its lowest warps at every turn, so
+        the long-lived particles of an uneven scan fill whole warps.
+        ``compact='two-phase'``: track the first turns/8 with the full
+        persistent grid, then relaunch only the survivors on a grid sized to
+        them (not for lattices that read ``turn``).  ``compact=False``: one
+        launch of the one-warp persistent kernel.  Loss turns and coordinates
+        are the same in every case."""
         pool = np.asarray(self.parameters, dtype=np.float64)
         seed_values, seed = self._c.seeds(pool)
         dprog = self._c.device(self.ctx, seed_values)
         coords = _coords_from_pool(pool, self._names, self.flags, self.dp)
         T, n = int(self.turns), coords.shape[0]
         if compact is None:
-            compact = T >= 512 and n >= 16384
-        if compact and self._uses_turn():
-            compact = False
+            compact = True
+        if compact == 'two-phase' and self._uses_turn():
+            compact = True
         flags = _track_flags(self.flags)
+        if compact is True:
+            before = self.ctx.warps_per_sm
+            self.ctx.set_tuning(self.COMPACT_WARPS_PER_SM)
+            try:
+                _, lost, final = capi.track(self.ctx, dprog, coords, T, capi.UFO_MODE_SA,
+                                            flags | capi.UFO_TRACK_COMPACT, seed=seed, slots=0)
+            finally:
+                self.ctx.set_tuning(before)
+            self.lost = lost
+            self.final = final
+            return
         if not compact:
             _, lost, final = capi.track(self.ctx, dprog, coords, T, capi.UFO_MODE_SA, flags,
                                         seed=seed, slots=0)
