@@ -35,6 +35,7 @@ SAMPLES = [('c2_track', 'c2', 16384, 100), ('c1_track', 'c1', 8192, 200)]
 
 
 def generate(ref_path):
+    sys.path.insert(0, HERE)  # the stand-in package oracle/refshim
     sys.path.insert(0, os.path.join(HERE, 'refshim'))
     sys.path.insert(0, ref_path)
     sys.dont_write_bytecode = True
