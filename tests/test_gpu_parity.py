@@ -365,12 +365,15 @@ def test_closed_orbit_parameter_batch():
             assert np.max(np.abs(co.orbits - ref)) < 1e-8
 
 
-@pytest.mark.parametrize('name', ['alba_kick_params', 'alba_thick_params'])
+@pytest.mark.parametrize('name', ['c1_seeds_kick', 'nlk_pulse'])
 def test_parameter_rerun_reuses_the_program(name):
     """The reference's workflow: one simulation object, new lattice values in
     ``.parameters`` between runs.  The second run takes the set-table path (the
     device program object is the same; only the per-seed constants are
-    re-uploaded) and reproduces the reference's golden tracks."""
+    re-uploaded) and reproduces the reference's golden tracks.  Cases: the C1
+    ring with per-particle misalignments and sextupole errors, and the HOWTO's
+    pulsed kicker with a per-particle trigger turn (cases whose particles keep
+    tracking, so that the first run's other values show in its tracks)."""
     c = H.case(name)
     import ufo_gb300 as u
     line = H.line_of(c)
