@@ -39,11 +39,7 @@ UFO_DEV double add(double a, double b) { return __dadd_rn(a, b); }
 UFO_DEV double sub(double a, double b) { return __dsub_rn(a, b); }
 UFO_DEV double dvd(double a, double b) { return __ddiv_rn(a, b); }
 UFO_DEV double fma_(double a, double b, double c) { return __fma_rn(a, b, c); }
-// a constant of the lattice tables: a generic load, so that the tables may
-// live in global memory or be staged in the CTA's shared memory (the
-// compacting kernel); pointers derived from kernel arguments still compile to
-// global loads
-UFO_DEV double ld(const double *p) { return *p; }
+UFO_DEV double ld(const double *p) { return __ldg(p); }
 
 // not finite: exponent field all ones (integer test, no FP64 pipe)
 UFO_DEV bool nf(double v) { return (__double2hiint(v) & 0x7ff00000) == 0x7ff00000; }

@@ -48,9 +48,7 @@ struct TrackArgs {
   uint32_t *lost;
   double *final_state;
   unsigned long long *queue;  // particles handed out so far
-  int stage;  // compacting kernel: STAGE_OPS / STAGE_TABLE staged in shared memory
 };
-constexpr int STAGE_OPS = 1, STAGE_TABLE = 2;
 
 UFO_DEV void load_particle(State &s, const TrackArgs &a, int64_t p) {
   const double *c = a.coords + p * 6;
@@ -89,11 +87,10 @@ UFO_DEV void observe(const State &s, const TrackArgs &a, int64_t p, int k) {
 // elements, kicks, alignments, constant edges, circular apertures and
 // observation points (chosen on the host); it carries far fewer live values.
 template <bool FMA, bool FULL>
-UFO_DEV void one_turn(State &s, const TrackArgs &a, const Op *ops, const double *tab,
-                      int64_t p) {
+UFO_DEV void one_turn(State &s, const TrackArgs &a, const double *tab, int64_t p) {
   for (int i = 0; i < a.n_ops; ++i) {
-    const int4 w0 = *reinterpret_cast<const int4 *>(ops + i);
-    const int4 w1 = *(reinterpret_cast<const int4 *>(ops + i) + 1);
+    const int4 w0 = __ldg(reinterpret_cast<const int4 *>(a.ops + i));
+    const int4 w1 = __ldg(reinterpret_cast<const int4 *>(a.ops + i) + 1);
     const Op op{w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
     const double *c = tab + op.toff;
     switch (op.kind) {
@@ -197,7 +194,6 @@ __global__ void __launch_bounds__(32) track_kernel(TrackArgs a) {
   State s{};
   int target = 0;
   const double *tab = a.table;
-  const Op *ops = a.ops;
   while (true) {
     // lanes without a particle take the next ones from the queue
     const unsigned need = __ballot_sync(ALL, p < 0 && !exhausted);
@@ -229,7 +225,7 @@ __global__ void __launch_bounds__(32) track_kernel(TrackArgs a) {
     }
     if (__all_sync(ALL, p < 0)) break;
     if (p >= 0) {
-      one_turn<FMA, FULL>(s, a, ops, tab, p);
+      one_turn<FMA, FULL>(s, a, tab, p);
       const bool lost = is_lost(s, a.mode);
       if (!lost) ++s.turn;
       if (lost || s.turn >= target) {
@@ -268,9 +264,7 @@ constexpr int CTA_MAX_WARPS = 16;
 
 template <bool FMA, bool FULL>
 __global__ void __launch_bounds__(CTA_MAX_WARPS * 32, 1) track_kernel_cta(TrackArgs a) {
-  // dynamic shared memory: one Parked slot per thread, then (when staged)
-  // the opcode table and the single seed's constant row
-  extern __shared__ Parked parked[];
+  extern __shared__ Parked parked[];  // one slot per thread of the CTA
   // lanes with a particle per warp, double-buffered by barrier phase (a warp
   // one phase ahead writes the other buffer)
   __shared__ int warp_active[2][CTA_MAX_WARPS];
@@ -281,32 +275,12 @@ __global__ void __launch_bounds__(CTA_MAX_WARPS * 32, 1) track_kernel_cta(TrackA
   const unsigned lt_mask = (1u << lane) - 1u;
   volatile int *flag = &exhausted_flag;
   if (threadIdx.x == 0) *flag = 0;
-  // stage the lattice: the warp-uniform opcode stream, and the constant row
-  // when every particle uses the same one, are read by every warp at every
-  // op of every turn; one copy per CTA serves them all from shared memory
-  const Op *ops = a.ops;
-  const double *table = a.table;
-  {
-    char *after = reinterpret_cast<char *>(parked + blockDim.x);
-    if (a.stage & STAGE_OPS) {
-      int4 *dst = reinterpret_cast<int4 *>(after);
-      const int4 *src = reinterpret_cast<const int4 *>(a.ops);
-      for (int i = threadIdx.x; i < 2 * a.n_ops; i += blockDim.x) dst[i] = src[i];
-      ops = reinterpret_cast<const Op *>(after);
-      after += sizeof(Op) * static_cast<size_t>(a.n_ops);
-    }
-    if (a.stage & STAGE_TABLE) {
-      double *dst = reinterpret_cast<double *>(after);
-      for (int64_t i = threadIdx.x; i < a.stride; i += blockDim.x) dst[i] = a.table[i];
-      table = dst;
-    }
-  }
   __syncthreads();
   int64_t p = -1;
   int sd = 0;
   State s{};
   int target = 0;
-  const double *tab = table;
+  const double *tab = a.table;
   // ---- phase A: refill from the counter, no barrier
   bool exhausted = false;
   while (true) {
@@ -329,7 +303,7 @@ __global__ void __launch_bounds__(CTA_MAX_WARPS * 32, 1) track_kernel_cta(TrackA
           load_particle(s, a, p);
           target = a.pturns ? a.pturns[p] : a.turns;
           sd = a.seed ? a.seed[p] : 0;
-          tab = table + static_cast<int64_t>(sd) * a.stride;
+          tab = a.table + static_cast<int64_t>(sd) * a.stride;
           if (sd < 0 || sd >= a.n_seeds) {  // seed outside the table: not tracked
             if (a.lost) a.lost[p] = 0xffffffffu;
             p = -1;
@@ -342,7 +316,7 @@ __global__ void __launch_bounds__(CTA_MAX_WARPS * 32, 1) track_kernel_cta(TrackA
     }
     if (exhausted) break;  // warp-uniform
     if (p >= 0) {  // a lane's particle needs no refill this turn
-      one_turn<FMA, FULL>(s, a, ops, tab, p);
+      one_turn<FMA, FULL>(s, a, tab, p);
       const bool lost = is_lost(s, a.mode);
       if (!lost) ++s.turn;
       if (lost || s.turn >= target) {
@@ -382,12 +356,12 @@ __global__ void __launch_bounds__(CTA_MAX_WARPS * 32, 1) track_kernel_cta(TrackA
         p = d.p;
         target = d.target;
         sd = d.seed;
-        tab = table + static_cast<int64_t>(sd) * a.stride;
+        tab = a.table + static_cast<int64_t>(sd) * a.stride;
       }
       // the slots are rewritten only after the next phase's barrier
     }
     if (p >= 0) {
-      one_turn<FMA, FULL>(s, a, ops, tab, p);
+      one_turn<FMA, FULL>(s, a, tab, p);
       const bool lost = is_lost(s, a.mode);
       if (!lost) ++s.turn;
       if (lost || s.turn >= target) {
@@ -413,9 +387,8 @@ __global__ void __launch_bounds__(128) track_plain_kernel(TrackArgs a) {
     return;
   }
   const double *tab = a.table + sd * a.stride;
-  const Op *ops = a.ops;
   while (s.turn < target) {
-    one_turn<FMA, FULL>(s, a, ops, tab, p);
+    one_turn<FMA, FULL>(s, a, tab, p);
     if (is_lost(s, a.mode)) break;
     ++s.turn;
   }
@@ -438,7 +411,7 @@ UFO_DEV double co_residual(const double *v, const TrackArgs &a, const double *ta
   s.z = 0.0; s.dp = 0.0; s.o = 1.0; s.opdp = 1.0;
   s.turn = 0;
   s.bad_o = false;
-  one_turn<false, FULL>(s, a, a.ops, tab, 0);
+  one_turn<false, FULL>(s, a, tab, 0);
   double r = mul(sub(v[0], s.x), sub(v[0], s.x));
   r = add(r, mul(sub(v[1], s.px), sub(v[1], s.px)));
   r = add(r, mul(sub(v[2], s.y), sub(v[2], s.y)));
@@ -623,9 +596,6 @@ int cuda_fail(cudaError_t e, const char *what) {
 // at the same time serialise on this mutex
 std::mutex g_setup_mutex;
 bool g_const_ready[64] = {};
-// dynamic shared memory a compacting-kernel CTA may use on each device (the
-// opt-in maximum per block, less the kernel's static shared memory)
-size_t g_smem_limit[64] = {};
 
 // Upload the constant tables to the current device, once per device.
 int ensure_constants(int device) {
@@ -643,22 +613,6 @@ int ensure_constants(int device) {
     rf[k] = 1.0 / fact;
   }
   UFO_CUDA(cudaMemcpyToSymbol(ufo::c_rcp_fact, rf, sizeof rf));
-  int optin = 0;
-  UFO_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
-  const size_t limit = optin > 4096 ? static_cast<size_t>(optin) - 4096 : 0;
-  UFO_CUDA(cudaFuncSetAttribute(ufo::track_kernel_cta<false, false>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(limit)));
-  UFO_CUDA(cudaFuncSetAttribute(ufo::track_kernel_cta<false, true>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(limit)));
-  UFO_CUDA(cudaFuncSetAttribute(ufo::track_kernel_cta<true, false>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(limit)));
-  UFO_CUDA(cudaFuncSetAttribute(ufo::track_kernel_cta<true, true>,
-                                cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                static_cast<int>(limit)));
-  g_smem_limit[device] = limit;
   g_const_ready[device] = true;
   return UFO_OK;
 }
@@ -826,7 +780,7 @@ int validate_ops(const int32_t *ops, int n_ops, int64_t stride, int n_dumps,
 // The launch shared by every entry point: fill the kernel arguments and start
 // the persistent (or plain) kernel on `stream`; `queue` is the work counter.
 int launch_kernels(ufo::TrackArgs &a, bool full, int sm_count, int warps_per_sm,
-                   size_t smem_limit, cudaStream_t stream) {
+                   cudaStream_t stream) {
   const bool fma = a.flags & UFO_TRACK_FMA;
   if (a.flags & UFO_TRACK_PLAIN) {
     const unsigned blocks = static_cast<unsigned>((a.n + 127) / 128);
@@ -846,19 +800,7 @@ int launch_kernels(ufo::TrackArgs &a, bool full, int sm_count, int warps_per_sm,
                                                                           : warps_per_sm;
     if (ctas * wpc > warps) wpc = static_cast<int>((warps + ctas - 1) / ctas);
     const unsigned g = static_cast<unsigned>(ctas), tpb = static_cast<unsigned>(wpc * 32);
-    size_t smem = sizeof(ufo::Parked) * tpb;
-    // stage what fits: the opcode table, then a single seed's constant row
-    a.stage = 0;
-    const size_t ops_b = sizeof(ufo::Op) * static_cast<size_t>(a.n_ops);
-    const size_t tab_b = sizeof(double) * static_cast<size_t>(a.stride);
-    if (smem + ops_b <= smem_limit) {
-      a.stage |= ufo::STAGE_OPS;
-      smem += ops_b;
-    }
-    if (a.n_seeds == 1 && smem + tab_b <= smem_limit) {
-      a.stage |= ufo::STAGE_TABLE;
-      smem += tab_b;
-    }
+    const size_t smem = sizeof(ufo::Parked) * tpb;
     if (fma)
       full ? ufo::track_kernel_cta<true, true><<<g, tpb, smem, stream>>>(a)
            : ufo::track_kernel_cta<true, false><<<g, tpb, smem, stream>>>(a);
@@ -909,7 +851,6 @@ ufo::TrackArgs make_args(const ufo::Op *ops, int n_ops, const double *table, int
   a.lost = d_lost;
   a.final_state = d_final;
   a.queue = queue;
-  a.stage = 0;
   return a;
 }
 
@@ -921,8 +862,7 @@ int launch_track(ufo_ctx *ctx, const ufo_prog *prog, const double *d_coords, con
   ufo::TrackArgs a = make_args(prog->ops, prog->n_ops, prog->table, prog->stride, prog->n_seeds,
                                prog->n_dumps, d_coords, d_seed, d_pturns, n, turns, mode, flags,
                                slots, every, d_tracks, d_lost, d_final, ctx->queue);
-  const int rc = launch_kernels(a, prog->full, ctx->sm_count, ctx->warps_per_sm,
-                                g_smem_limit[ctx->device], stream);
+  const int rc = launch_kernels(a, prog->full, ctx->sm_count, ctx->warps_per_sm, stream);
   if (rc == UFO_OK) ctx->launches.fetch_add(1);
   return rc;
 }
@@ -1306,7 +1246,7 @@ extern "C" int ufo_track_noalloc(const int32_t *ops, int n_ops, const double *d_
                                d_coords, d_seed, d_pturns, n, turns, mode,
                                flags & ~UFO_TRACK_PLAIN, slots, every, d_tracks, d_lost, d_final,
                                &d.scratch->queue);
-  return launch_kernels(a, needs_full(ops, n_ops), d.sm_count, 16, g_smem_limit[device], st);
+  return launch_kernels(a, needs_full(ops, n_ops), d.sm_count, 16, st);
 }
 
 // ===================================================== tuning and graphs
