@@ -70,6 +70,8 @@ def parse():
                     help='print the FP64-pipe probe table (latency, occupancy, active lanes)')
     ap.add_argument('--c5-skip-multiturn', action='store_true',
                     help='C5: optics gradients only (for profiling captures)')
+    ap.add_argument('--c3-grid', type=int, default=256,
+                    help='C3: radial and angular grid points (256: the benchmark grid)')
     ap.add_argument('--op-mix', action='store_true',
                     help='one small launch per element type and mode (for an ncu op-mix capture)')
     ap.add_argument('--no-c4', action='store_true',
@@ -560,7 +562,7 @@ def bench_c3(args):
     lib = capi.load()
     ring = W.c3_ring(u)
     n_elem = len(ring.flatten())
-    grid = W.c3_grid()
+    grid = W.c3_grid(args.c3_grid, args.c3_grid)
     n, T = grid.shape[0], 2048
     flags = u.KICK | (u.FMA if args.mode == 'fma' else 0)
     tflags = capi.UFO_TRACK_FMA if args.mode == 'fma' else 0
@@ -576,22 +578,26 @@ def bench_c3(args):
     lost = torch.empty(n, dtype=torch.int32, device=dev)
     final = torch.empty((n, 6), dtype=torch.float64, device=dev)
 
-    def launch(coords, plain):
+    kinds = {'compact': capi.UFO_TRACK_COMPACT, 'persistent': 0, 'plain': capi.UFO_TRACK_PLAIN}
+
+    def launch(coords, kind):
         capi.check(lib.ufo_track_device(
             ctx.handle, dprog.handle, capi.ptr(coords.data_ptr()), None, None, n, T,
-            capi.UFO_MODE_SA, tflags | (capi.UFO_TRACK_PLAIN if plain else 0), 0, 1, None,
+            capi.UFO_MODE_SA, tflags | kinds[kind], 0, 1, None,
             capi.ptr(lost.data_ptr()), capi.ptr(final.data_ptr()), capi.ptr(stream.cuda_stream)))
 
-    def timed(order, plain, steps):
+    def timed(order, kind, steps):
         coords = inputs[order]
+        # the compacting kernel at StableAperture's resident warps per SM
+        ctx.set_tuning(u.StableAperture.COMPACT_WARPS_PER_SM if kind == 'compact' else 16)
         for _ in range(args.warmup):
-            launch(coords, plain)
+            launch(coords, kind)
         torch.cuda.synchronize()
         l0 = ctx.launches()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
         for _ in range(steps):
-            launch(coords, plain)
+            launch(coords, kind)
         e1.record(stream)
         torch.cuda.synchronize()
         lo = lost.cpu().numpy().view(np.uint32).astype(np.int64)
@@ -605,11 +611,12 @@ def bench_c3(args):
     clocks.start()
     runs = {}
     for order in ('sorted', 'shuffled', 'amplitude'):
-        for plain in (False, True):
-            runs[(order, plain)] = timed(order, plain, args.steps if not plain else
-                                         max(1, args.steps // 2))
-    ms_p, launches, lost_p = runs[('sorted', False)]
-    ms_plain, _, lost_plain = runs[('sorted', True)]
+        for kind in kinds:
+            runs[(order, kind)] = timed(order, kind, args.steps)
+    ctx.set_tuning(16)
+    ms_p, launches, lost_p = runs[('sorted', 'compact')]
+    ms_pers = runs[('sorted', 'persistent')][0]
+    ms_plain = runs[('sorted', 'plain')][0]
     # the public API: StableAperture.run with in-kernel compaction (default),
     # two-phase compaction and none (host buffers in and out, wall clock)
     api = {}
@@ -635,9 +642,10 @@ def bench_c3(args):
             'unit': 'particle*element*turns/s', 'n_gpus': 1, 'steps': args.steps,
             'warmup': args.warmup, 'ms_per_step': ms_p, 'higher_is_better': True,
             'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic',
-            'config': {'workload': 'C3 dynamic aperture: 256x256 polar grid (r 0-25 mm, '
-                                   'angle 0-pi/2) x dp {-2%, 0, +2%}, 2048 turns, SA loss '
-                                   'test, C1 ring with 10 mm apertures and C4 seed-0 errors',
+            'config': {'workload': f'C3 dynamic aperture: {args.c3_grid}x{args.c3_grid} polar '
+                                   'grid (r 0-25 mm, angle 0-pi/2) x dp {-2%, 0, +2%}, 2048 '
+                                   'turns, SA loss test, C1 ring with 10 mm apertures and C4 '
+                                   'seed-0 errors',
                        'particles': n, 'turns': T, 'elements': n_elem, 'mode': args.mode,
                        'l2': 'inputs resident; each launch re-reads 9.4 MB of coordinates'},
             'roofline': {'bound': 'fp64', 'achieved': fl * tracked / (ms_p / 1e3) / 1e9,
@@ -647,19 +655,18 @@ def bench_c3(args):
                          'peak_source': 'measured live: ufo_fp64_peak'},
             'survival_fraction': surv,
             'particle_turns_tracked': int(tracked),
+            'kernel': 'CTA-compacting persistent kernel, one launch, '
+                      f'{u.StableAperture.COMPACT_WARPS_PER_SM} warps per SM',
+            'one_warp_persistent': {'value': pet / (ms_pers / 1e3), 'ms': ms_pers},
             'plain_one_thread_per_particle': {'value': pet / (ms_plain / 1e3), 'ms': ms_plain},
-            'speedup_persistent_vs_plain': ms_plain / ms_p,
+            'speedup_compact_vs_plain': ms_plain / ms_p,
+            'speedup_compact_vs_one_warp_persistent': ms_pers / ms_p,
             'shuffled_order': {
-                'persistent': pet / (runs[('shuffled', False)][0] / 1e3),
-                'plain': pet / (runs[('shuffled', True)][0] / 1e3),
-                'speedup_persistent_vs_plain':
-                    runs[('shuffled', True)][0] / runs[('shuffled', False)][0],
-                'note': 'the same grid in a seeded random order: warps of the plain '
-                        'kernel mix survivors and early losses'},
+                k: pet / (runs[('shuffled', k)][0] / 1e3) for k in kinds},
             'amplitude_order': {
-                'persistent': pet / (runs[('amplitude', False)][0] / 1e3),
-                'plain': pet / (runs[('amplitude', True)][0] / 1e3),
-                'note': 'the same grid, largest amplitude (then |dp|) first'},
+                k: pet / (runs[('amplitude', k)][0] / 1e3) for k in kinds},
+            'order_note': 'the same grid in a seeded random order (warps of the plain kernel '
+                          'mix survivors and early losses) and largest amplitude first',
             'stable_aperture_api': {
                 'one_phase_no_compaction': {'value': pet / api[False][0], 's': api[False][0]},
                 'two_phase_compaction': {
