@@ -56,8 +56,17 @@ def test_loss_turns_vs_reference(name):
     if H.program_is_exact(_prog(s)):
         assert np.array_equal(s.lost, ref)
     else:
-        # per-particle transcendentals (wire): chaotic particles may differ
-        assert np.mean(s.lost == ref) > 0.95
+        # per-particle transcendentals (wire) use CUDA's libm, which may differ
+        # from the C library in the last bit.  A particle whose loss turn the
+        # oracle keeps when its start moves by +-1e-15 (relative; several ulps,
+        # more than a libm difference) must have the reference's loss turn;
+        # only particles on a loss boundary that a last-bit change moves are
+        # exempt
+        o = H.oracle_case(c)['lost']
+        stable = (H.oracle_case(c, perturb=1e-15)['lost'] == o) & \
+            (H.oracle_case(c, perturb=-1e-15)['lost'] == o)
+        assert stable.mean() >= 0.9, stable.mean()
+        assert np.array_equal(s.lost[stable], ref[stable])
 
 
 def test_fodo_matches_madx_golden():

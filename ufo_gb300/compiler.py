@@ -425,12 +425,12 @@ class _Lowerer:
         else:
             # what the FMA-mode kernel executes (csrc/ops.cuh: teapot_v): drifts 2
             # FMA each; the kick strength formed once per element (quadrupole
-            # t = K o: 1 mul; sextupole t = (K o) 0.5 and 2t: 3 operations); per
+            # t = K o: 1 mul; sextupole K o and t = (K o) 0.5: 2 muls); per
             # slice the kick (quadrupole 2 FMA, sextupole 2 mul + 3 FMA, general
             # the power-series Horner) and the weak term (1 FMA)
             pat = 0 if nsk else 1 if (nn == 2 and mn == 2) else 2 if (nn == 3 and mn == 4) \
                 else 3 if mn == 0 else 0
-            per_elem = {0: 0, 1: 1, 2: 3, 3: 0}[pat]
+            per_elem = {0: 0, 1: 1, 2: 2, 3: 0}[pat]
             kick = {0: ks.flops_fast() if (mn | ms) else 0, 1: 4, 2: 8, 3: 0}[pat]
             op.flops_fast = 4 * (slices + 1) + per_elem + slices * (kick + wflops)
         self.emit(op)

@@ -553,8 +553,11 @@ UFO_DEV void teapot_v(State &s, const Op &op, const double *c) {
   const double o1 = achro ? 1.0 : s.o;
   double t = 0.0, t2 = 0.0;
   if (PAT == 1) t = mul(ld(ck), o1);
-  if (PAT == 2) t = mul(mul(ld(ck), o1), 0.5);
-  if (FMA && PAT == 2) t2 = add(t, t);
+  if (PAT == 2) {  // t = (K*o)*0.5; the FMA form's 2t is K*o itself (exact)
+    const double ko = mul(ld(ck), o1);
+    t = mul(ko, 0.5);
+    if (FMA) t2 = ko;
+  }
   // general kicks of FMA programs: the dense series after every other constant
   const double *ps = nullptr;
   if (FMA && PAT == 0 && (op.flags & F_PSER)) {
