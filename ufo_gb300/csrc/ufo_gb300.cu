@@ -88,20 +88,9 @@ UFO_DEV void observe(const State &s, const TrackArgs &a, int64_t p, int k) {
 // observation points (chosen on the host); it carries far fewer live values.
 template <bool FMA, bool FULL>
 UFO_DEV void one_turn(State &s, const TrackArgs &a, const double *tab, int64_t p) {
-  // the next op's words are fetched while the current op computes: the
-  // warp-uniform dispatch does not wait on a load at every op
-  const int4 *words = reinterpret_cast<const int4 *>(a.ops);
-  int4 n0 = make_int4(0, 0, 0, 0), n1 = n0;
-  if (a.n_ops > 0) {
-    n0 = __ldg(words);
-    n1 = __ldg(words + 1);
-  }
   for (int i = 0; i < a.n_ops; ++i) {
-    const int4 w0 = n0, w1 = n1;
-    if (i + 1 < a.n_ops) {
-      n0 = __ldg(words + 2 * (i + 1));
-      n1 = __ldg(words + 2 * (i + 1) + 1);
-    }
+    const int4 w0 = __ldg(reinterpret_cast<const int4 *>(a.ops + i));
+    const int4 w1 = __ldg(reinterpret_cast<const int4 *>(a.ops + i) + 1);
     const Op op{w0.x, w0.y, w0.z, w0.w, w1.x, w1.y, w1.z, w1.w};
     const double *c = tab + op.toff;
     switch (op.kind) {
