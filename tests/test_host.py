@@ -180,7 +180,7 @@ def test_fma_drift_merging_conserves_length_and_flops():
 
     for ring in (W.c2_ring(u), W.c3_ring(u)):
         strict = C.compile_line(ring, u.KICK, where=[-1])
-        fma = C.compile_line(ring, u.KICK | u.FMA, where=[-1])
+        fma = C.compile_line(ring, u.KICK | u.FMA, where=[-1], linearize=False)
         assert len(fma.ops) < len(strict.ops)
         merged = sum(int(r[0]) == C.OP_DRIFT for r in strict.ops) - \
             sum(int(r[0]) == C.OP_DRIFT for r in fma.ops)
@@ -244,3 +244,55 @@ def test_fma_programs_append_dense_power_series_for_general_kicks():
                     assert np.all(got == 0.0) and not np.any(np.signbit(got))
     assert n_series > 0
     assert math.isclose(rf[5], 1 / 120, rel_tol=1e-15)
+
+
+@pytest.mark.parametrize('yoshida', [False, True])
+def test_fma_linear_elements_compose_their_drifts_and_weak_kicks(yoshida):
+    """FMA programs replace each kick-free teapot (or Yoshida) element, here
+    the C2 ring's bends with their merged neighbouring drifts, by one linear
+    op: a 2x2 matrix for (x, px) and a drift for (y, py), composed on the host.
+    Applied to test vectors it equals the element's own sequence of drifts and
+    weak-focusing kicks to rounding."""
+    ring = W.c2_ring(u)
+    fl = u.KICK | u.FMA | (u.YOSHIDA if yoshida else 0)
+    lin = C.compile_line(ring, fl, where=[-1])
+    ref = C.compile_line(ring, fl, where=[-1], linearize=False)
+    assert len(lin.ops) == len(ref.ops)
+    assert lin.flops == ref.flops and lin.flops_fast < ref.flops_fast
+    rng = np.random.default_rng(3)
+    v = rng.standard_normal((4, 16)) * np.array([[1e-3], [1e-4], [1e-3], [1e-4]])
+    n = 0
+    for a, b in zip(lin.ops, ref.ops):
+        if int(a[0]) != C.OP_LINEAR:  # the same op (its table offset may move)
+            assert np.array_equal(np.delete(a, 2), np.delete(b, 2))
+            continue
+        n += 1
+        assert int(b[0]) == C.OP_TEAPOT
+        m = lin.table[0, int(a[2]):int(a[2]) + 5]
+        c = ref.table[0, int(b[2]):]
+        N, fl_b = int(b[3]), int(b[1])
+        x, px, y, py = v.copy()
+        if fl_b & C.F_YOSHIDA:
+            wk = c[7] if fl_b & C.F_WEAK else 0.0
+            for _ in range(N):
+                x, y = x + px * c[0], y + py * c[0]
+                for k in range(3):
+                    px = px - x * (wk * c[4 + k])
+                    x, y = x + px * c[1 + k], y + py * c[1 + k]
+        else:
+            fi = (fl_b >> C.SH_FINNER) & 3
+            Li = c[1] if fi == C.DF_MUL else c[4]
+            ck = 1 + (0 if N <= 1 else (4 if fi == C.DF_DIV else 1))
+            wk = c[ck] if fl_b & C.F_WEAK else 0.0
+            Lx = c[ck + (1 if fl_b & C.F_WEAK else 0)] if fl_b & C.F_SPLITO else c[0]
+            x, y = x + px * c[0], y + py * c[0]
+            for sl in range(N):
+                px = px - x * wk
+                L = Li if sl < N - 1 else Lx
+                x, y = x + px * L, y + py * L
+        xl = m[0] * v[0] + m[1] * v[1]
+        pxl = m[2] * v[0] + m[3] * v[1]
+        yl = v[2] + v[3] * m[4]
+        for got, want in ((xl, x), (pxl, px), (yl, y)):
+            assert np.max(np.abs(got - want)) <= 1e-15 * np.max(np.abs(want)) + 1e-19
+    assert n == 128

@@ -17,7 +17,7 @@ namespace ufo {
 
 enum : int {
   OP_NOP = 0, OP_DRIFT, OP_KICK, OP_TEAPOT, OP_ALIGN, OP_EDGE, OP_THICKQ, OP_THICKB, OP_WIRE,
-  OP_APERTURE, OP_OBSERVE, OP_DYNKICK
+  OP_APERTURE, OP_OBSERVE, OP_DYNKICK, OP_LINEAR
 };
 enum : int { DF_MUL = 0, DF_MUL2 = 1, DF_DIV = 2 };
 enum : int {

@@ -165,6 +165,16 @@ UFO_DEV void one_turn(State &s, const TrackArgs &a, const double *tab, int64_t p
       case OP_OBSERVE:
         observe(s, a, p, op.i0);
         break;
+      case OP_LINEAR: {
+        // a kick-free teapot element of an FMA program composed on the host:
+        // (x, px) through a 2x2 matrix, (y, py) through a drift
+        const double m11 = ld(c), m12 = ld(c + 1), m21 = ld(c + 2), m22 = ld(c + 3);
+        const double x0 = s.x;
+        s.x = fma_(m11, x0, mul(m12, s.px));
+        s.px = fma_(m21, x0, mul(m22, s.px));
+        s.y = fma_(s.py, ld(c + 4), s.y);
+        break;
+      }
       case OP_DYNKICK:
         if (FULL) {
           const PxPy r = dynkick_ool(s.x, s.px, s.y, s.py, s.z, s.dp, s.o, s.turn, op.i0, op.i1,
@@ -688,6 +698,8 @@ int64_t op_consts(const int32_t *w) {
     case ufo::OP_DYNKICK:
       if (w[3] < 0 || w[4] < 0 || w[3] > 32 || w[4] > 32 || w[5] < w[3] + w[4]) return -1;
       return w[5];
+    case ufo::OP_LINEAR:
+      return 5;
     default:
       return -1;
   }
@@ -758,7 +770,7 @@ int validate_ops(const int32_t *ops, int n_ops, int64_t stride, int n_dumps,
                  const double *table) {
   for (int i = 0; i < n_ops; ++i) {
     const int32_t *w = ops + i * UFO_OP_WORDS;
-    if (w[0] < ufo::OP_NOP || w[0] > ufo::OP_DYNKICK)
+    if (w[0] < ufo::OP_NOP || w[0] > ufo::OP_LINEAR)
       return fail(UFO_E_ARG, "op %d: unknown kind %d", i, w[0]);
     // an observation point writes slot (turn / every) * n_dumps + index
     if (w[0] == ufo::OP_OBSERVE && (w[3] < 0 || w[3] >= n_dumps))

@@ -105,7 +105,8 @@ class DiffProgram:
             vals = vals.reshape(-1, len(parameters))
         # the differentiator has its own (fused) arithmetic: it takes the FMA-mode
         # program, whose plain drifts are folded into the magnets' outer drifts
-        prog = C.compile_line(line, flags | FMA, parameters, [], seed_values=vals)
+        prog = C.compile_line(line, flags | FMA, parameters, [], seed_values=vals,
+                              linearize=False)
         self.prog = prog
         flat = line.flatten() if hasattr(line, 'flatten') else list(line)
         # element index -> (parameter slot, coefficient order)
