@@ -257,12 +257,18 @@ def test_fma_linear_elements_compose_their_drifts_and_weak_kicks(yoshida):
     fl = u.KICK | u.FMA | (u.YOSHIDA if yoshida else 0)
     lin = C.compile_line(ring, fl, where=[-1])
     ref = C.compile_line(ring, fl, where=[-1], linearize=False)
-    assert len(lin.ops) == len(ref.ops)
     assert lin.flops == ref.flops and lin.flops_fast < ref.flops_fast
+    # the bends' zero-angle edges (structural zeros) leave with them
+    linear_elems = {e for e, r in zip(lin.op_elem, lin.ops) if int(r[0]) == C.OP_LINEAR}
+    keep = [i for i, r in enumerate(ref.ops) if not (
+        int(r[0]) == C.OP_EDGE and ref.op_elem[i] in linear_elems and
+        not int(r[1]) & (C.F_T1 | C.F_T2 | C.F_RTPSI))]
+    assert len(keep) == len(lin.ops) < len(ref.ops)
+    ref_ops = ref.ops[keep]
     rng = np.random.default_rng(3)
     v = rng.standard_normal((4, 16)) * np.array([[1e-3], [1e-4], [1e-3], [1e-4]])
     n = 0
-    for a, b in zip(lin.ops, ref.ops):
+    for a, b in zip(lin.ops, ref_ops):
         if int(a[0]) != C.OP_LINEAR:  # the same op (its table offset may move)
             assert np.array_equal(np.delete(a, 2), np.delete(b, 2))
             continue

@@ -1030,7 +1030,7 @@ def _linearize(ops):
     coordinates, a linear map that does not depend on the particle's dp: its
     drifts and weak-focusing kicks compose on the host into one 2x2 matrix for
     (x, px) and one drift length for (y, py) (OP_LINEAR: 5 FP64 instructions
-    instead of 4 per slice).  The composition is formed per seed in FP64, so
+    instead of 4 per slice), and its zero-angle edges are dropped.  The composition is formed per seed in FP64, so
     results change in rounding only (tolerance parity, like the rest of FMA
     mode).  The reference count of the element is kept; the executed count is
     the op's own."""
@@ -1079,7 +1079,12 @@ def _linearize(ops):
         lin.flops = op.flops
         lin.flops_fast = 8  # x, px: a multiplication and an FMA each; y: one FMA
         out.append(lin)
-    return out
+    # the element's own zero edges (no face angle: their terms are structural
+    # zeros, kept only to poison px, py when x, y are not finite) go with it:
+    # the composed map already propagates non-finite values its own way
+    linear = {op.elem for op in out if op.kind == OP_LINEAR}
+    return [op for op in out if not (op.kind == OP_EDGE and op.elem in linear and
+                                     not op.flags & (F_T1 | F_T2 | F_RTPSI))]
 
 
 def _rcp_factorials(n):
