@@ -38,7 +38,10 @@ extern "C" {
 #define UFO_TRACK_FMA 1      /* fused multiply-add arithmetic (tolerance parity) */
 #define UFO_TRACK_FIVED 2    /* do not write z, dp into tracks (ufo/track.py:62-65) */
 #define UFO_TRACK_PLAIN 4    /* one thread per particle, no lane refill */
-#define UFO_TRACK_COMPACT 8  /* persistent CTAs that pack survivors into full warps */
+#define UFO_TRACK_COMPACT 8  /* persistent CTAs (one per SM, warps_per_sm warps, at most
+                                16) that pack survivors into full warps once every particle
+                                is handed out; PLAIN takes precedence.  Every kernel gives
+                                the same results bit for bit. */
 
 #define UFO_OP_WORDS 8
 
