@@ -1,11 +1,10 @@
 #!/usr/bin/env python
 """Benchmark: FP64 particle*element*turns/s on one GB300 (or N, weak scaling).
 
-Default workload (C2): 65,536 Gaussian particles through the 1024-element
-synthetic light-source ring (teapot, 4 slices; see ufo_gb300/workloads.py),
-10,000 turns.  A step is one launch tracking every particle 1,000 turns, so
-the default --steps 10 is the whole 10,000-turn job; each step continues from
-the previous step's coordinates.  Element = one entry of Line.flatten().
+Headline workload (C2): 65,536 Gaussian particles through the 1024-element
+synthetic light-source ring (teapot, 4 slices; see ufo_gb300/workloads.py).  A
+step is one launch tracking every particle 1,000 turns, each step continuing
+from the previous step's coordinates.  Element = one entry of Line.flatten().
 
 Printed (rank 0, one JSON line):
   value      device-resident inputs, CUDA events over exactly K steps, max
@@ -13,20 +12,25 @@ Printed (rank 0, one JSON line):
   e2e        the same K steps through the public API (Track.run with host
              numpy buffers: H2D of the coordinates, D2H of tracks/lost/final
              inside the timed region)
-  roofline   FP64-pipe bound: algorithmic FP64 flops per launch (compiler's
-             count of the reference expression, structural zeros removed)
-             over the average launch time, against the FP64 FMA peak measured
-             live on the same GPU
-  cpu_baseline  the reference's own generated kernel (oracle/_ref), or the
-             oracle port when that is absent, on a bounded sample on the host
-             cores
+  roofline   FP64-pipe bound: the FP64 work the kernel executes (compiler model
+             of its instruction mix, FMA = 2) over the mean launch time, against
+             the DFMA peak measured live on the same GPU; beside it the
+             reference expression's operation count over the same time and the
+             committed ncu figures (profiles/track_kernel_c2_ncu.json)
+  cpu_baseline  the reference's own generated kernel (oracle/_ref) under its
+             default fast-math options, or the oracle port when that is absent,
+             on a bounded sample on the host cores; cpu_baseline_strict_ieee the
+             same kernel built strict (the parity build)
+  strict, yoshida4  the same ring bit-identical to the reference, and with the
+             4th-order Yoshida integrator of the configuration as specified
+  c4, c3, c5 (one-rank runs only) the metric's other clauses: 512 batched error
+             seeds against one launch per seed, the dynamic-aperture scan with
+             in-kernel compaction, the adjoint against finite differences
 --impl reference times the reference's CPU implementation the same way.
 
-Other workloads (--workload): c3 dynamic-aperture scan (persistent vs plain
-kernel, sorted and shuffled grids), c4 batched error seeds (one autotuned
-CUDA-graph launch vs one launch per seed), c5 adjoint gradients against central
-finite differences (accuracy and device/wall cost).  The c2 line also carries
-the strict-mode (bit-identical) and Yoshida-4 measurements of the same ring.
+Other workloads (--workload) print one line each with more detail: c3 (every
+kernel and particle order, the StableAperture variants), c4, c5.  --op-mix runs
+one small launch per element type for an ncu instruction-mix capture.
 """
 import argparse
 import json
