@@ -76,6 +76,9 @@ def parse():
                     help='C5: optics gradients only (for profiling captures)')
     ap.add_argument('--c3-grid', type=int, default=256,
                     help='C3: radial and angular grid points (256: the benchmark grid)')
+    ap.add_argument('--c3-compact-warps', type=int, default=0,
+                    help='C3: resident warps per SM of the compacting kernel '
+                         '(0: StableAperture.COMPACT_WARPS_PER_SM)')
     ap.add_argument('--op-mix', action='store_true',
                     help='one small launch per element type and mode (for an ncu op-mix capture)')
     ap.add_argument('--no-c4', action='store_true',
@@ -593,7 +596,8 @@ def bench_c3(args):
     def timed(order, kind, steps):
         coords = inputs[order]
         # the compacting kernel at StableAperture's resident warps per SM
-        ctx.set_tuning(u.StableAperture.COMPACT_WARPS_PER_SM if kind == 'compact' else 16)
+        cw = args.c3_compact_warps or u.StableAperture.COMPACT_WARPS_PER_SM
+        ctx.set_tuning(cw if kind == 'compact' else 16)
         for _ in range(args.warmup):
             launch(coords, kind)
         torch.cuda.synchronize()
