@@ -48,6 +48,12 @@ struct TrackArgs {
   uint32_t *lost;
   double *final_state;
   unsigned long long *queue;  // particles handed out so far
+  // compacting kernel: chunks of 32 consecutive particles are handed out in
+  // the order c -> (c * spread) mod (n / 32) (spread coprime to n / 32; 0: in
+  // order; a last partial chunk comes last), so that a warp still takes
+  // neighbours (which tend to survive or be lost together) while the chunks of
+  // a region that survives are spread over every SM
+  unsigned long long spread;
 };
 
 UFO_DEV void load_particle(State &s, const TrackArgs &a, int64_t p) {
@@ -310,6 +316,10 @@ __global__ void __launch_bounds__(CTA_MAX_WARPS * 32, 1) track_kernel_cta(TrackA
         const int64_t q = static_cast<int64_t>(base) + __popc(need & lt_mask);
         if (q < a.n) {
           p = q;
+          const unsigned long long full = static_cast<unsigned long long>(a.n) / 32u;
+          const unsigned long long chunk = static_cast<unsigned long long>(q) / 32u;
+          if (a.spread && chunk < full)
+            p = static_cast<int64_t>(((chunk * a.spread) % full) * 32u + (q & 31));
           load_particle(s, a, p);
           target = a.pturns ? a.pturns[p] : a.turns;
           sd = a.seed ? a.seed[p] : 0;
@@ -789,6 +799,29 @@ int validate_ops(const int32_t *ops, int n_ops, int64_t stride, int n_dumps,
   return UFO_OK;
 }
 
+// Chunk hand-out order of the compacting kernel: c -> (c * m) mod n_chunks
+// with m coprime to the number of whole 32-particle chunks, near it / golden
+// ratio: a permutation whose early values sample the whole input evenly (a
+// dynamic-aperture grid is ordered by amplitude, and its surviving chunks
+// would otherwise all go to the first SMs to start).
+unsigned long long spread_multiplier(int64_t n_particles) {
+  const int64_t n = n_particles / 32;
+  if (n < 3) return 0;
+  unsigned long long m = static_cast<unsigned long long>(0.6180339887498949 * static_cast<double>(n));
+  const unsigned long long un = static_cast<unsigned long long>(n);
+  auto gcd = [](unsigned long long x, unsigned long long y) {
+    while (y) {
+      const unsigned long long t = x % y;
+      x = y;
+      y = t;
+    }
+    return x;
+  };
+  if (m < 1) m = 1;
+  while (gcd(m, un) != 1) ++m;  // ends: m = n - 1 is coprime to n
+  return m;
+}
+
 // The launch shared by every entry point: fill the kernel arguments and start
 // the persistent (or plain) kernel on `stream`; `queue` is the work counter.
 int launch_kernels(ufo::TrackArgs &a, bool full, int sm_count, int warps_per_sm,
@@ -811,6 +844,7 @@ int launch_kernels(ufo::TrackArgs &a, bool full, int sm_count, int warps_per_sm,
     int wpc = warps_per_sm < 1 ? 1 : warps_per_sm > ufo::CTA_MAX_WARPS ? ufo::CTA_MAX_WARPS
                                                                           : warps_per_sm;
     if (ctas * wpc > warps) wpc = static_cast<int>((warps + ctas - 1) / ctas);
+    a.spread = spread_multiplier(a.n);
     const unsigned g = static_cast<unsigned>(ctas), tpb = static_cast<unsigned>(wpc * 32);
     const size_t smem = sizeof(ufo::Parked) * tpb;
     if (fma)
@@ -863,6 +897,7 @@ ufo::TrackArgs make_args(const ufo::Op *ops, int n_ops, const double *table, int
   a.lost = d_lost;
   a.final_state = d_final;
   a.queue = queue;
+  a.spread = 0;
   return a;
 }
 
