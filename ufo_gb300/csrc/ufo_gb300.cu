@@ -806,7 +806,9 @@ int validate_ops(const int32_t *ops, int n_ops, int64_t stride, int n_dumps,
 // would otherwise all go to the first SMs to start).
 unsigned long long spread_multiplier(int64_t n_particles) {
   const int64_t n = n_particles / 32;
-  if (n < 3) return 0;
+  // chunk * m < n^2 must fit 64 bits: beyond 2^31 chunks (far more particles
+  // than device memory holds) the chunks go out in order
+  if (n < 3 || n >= (int64_t{1} << 31)) return 0;
   unsigned long long m = static_cast<unsigned long long>(0.6180339887498949 * static_cast<double>(n));
   const unsigned long long un = static_cast<unsigned long long>(n);
   auto gcd = [](unsigned long long x, unsigned long long y) {
