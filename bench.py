@@ -625,8 +625,8 @@ def bench_c3(args):
     ms_p, launches, lost_p = runs[('sorted', 'compact')]
     ms_pers = runs[('sorted', 'persistent')][0]
     ms_plain = runs[('sorted', 'plain')][0]
-    # the public API: StableAperture.run with in-kernel compaction (default),
-    # two-phase compaction and none (host buffers in and out, wall clock)
+    # the public API: StableAperture.run with two-phase compaction (default),
+    # in-kernel compaction and none (host buffers in and out, wall clock)
     api = {}
     for compact in (False, 'two-phase', True):
         sa = u.StableAperture(ring, flags=flags | u.DOUBLE_PRECISION, turns=T, particles=n,
@@ -684,17 +684,18 @@ def bench_c3(args):
                 'in_kernel_compaction': {'value': pet / api[True][0], 's': api[True][0]},
                 'note': 'StableAperture.run end to end (host buffers); the two-phase run '
                         'tracks turns/8 on the full grid, then only the survivors on a grid '
-                        'sized to them; the default packs survivors inside one launch'},
+                        'sized to them (the default); the in-kernel form packs survivors and '
+                        'evens out the CTAs inside one launch'},
             'identical_loss_turns': bool(all(np.array_equal(lost_p, r[2])
                                              for r in runs.values()) and
                                          all(np.array_equal(a[1], lost_p)
                                              for a in api.values())),
             'gpu_launches': launches,
-            'e2e': {'value': pet / api[True][0], 'unit': 'particle*element*turns/s',
+            'e2e': {'value': pet / api['two-phase'][0], 'unit': 'particle*element*turns/s',
                     'h2d_bytes_per_step': n * 6 * 8,
                     'd2h_bytes_per_step': n * (6 * 8 + 4),
-                    'api': 'ufo_gb300.StableAperture(...).run() (in-kernel compaction, host '
-                           'buffers)'}}
+                    'api': 'ufo_gb300.StableAperture(...).run() (two-phase compaction, the '
+                           'default; host buffers)'}}
     if clk:
         line['clocks'] = clk
     print(json.dumps(line), flush=True)
@@ -779,7 +780,8 @@ def c3_measure(ctx, stream, mode, reps=2):
                     '{-2%, 0, +2%} = 196,608 particles, 2,048 turns, SA loss test, C1 ring with '
                     '10 mm apertures and C4 seed-0 errors',
         'value': best['value'], 'unit': 'particle*element*turns/s', 'mode': mode,
-        'kernel': 'CTA-compacting persistent kernel, one launch',
+        'kernel': 'CTA-compacting persistent kernel (CTAs exchange particles through a pool), '
+                  f'one launch, {u.StableAperture.COMPACT_WARPS_PER_SM} warps per SM',
         'ms_per_launch': best['ms'], 'particle_turns_tracked': int(tracked),
         'survival_fraction': float(np.mean(lost_strict >= T)),
         'roofline': {'bound': 'fp64', 'achieved': achieved, 'peak': peak, 'unit': 'GFLOP/s',
@@ -795,7 +797,8 @@ def c3_measure(ctx, stream, mode, reps=2):
                            'the loss turns of the strict (bit-identical) arithmetic',
         'e2e': {'value': pet / e2e_s, 'unit': 'particle*element*turns/s', 's': e2e_s,
                 'h2d_bytes_per_step': n * 6 * 8, 'd2h_bytes_per_step': n * (6 * 8 + 4),
-                'api': 'ufo_gb300.StableAperture(...).run() (host buffers)'}}
+                'api': 'ufo_gb300.StableAperture(...).run() (two-phase compaction, the default; '
+                       'host buffers)'}}
 
 
 def _normwise(g, fd):

@@ -201,10 +201,11 @@ def test_c3_full_grid_subset_loss_turns_vs_oracle():
 
 
 def test_stable_aperture_two_phase_is_identical():
-    """StableAperture's compaction (first turns/8 on the full grid, the
-    survivors on a grid sized to them) and its in-kernel compaction (the
-    default) give the loss turns and coordinates of one plain persistent run,
-    bit for bit, in strict and FMA modes."""
+    """StableAperture's two-phase compaction (the default: first turns/8 on
+    the full grid, the survivors on a grid sized to them) and its in-kernel
+    compaction (CTAs packing and exchanging particles) give the loss turns and
+    coordinates of one plain persistent run, bit for bit, in strict and FMA
+    modes."""
     import ufo_gb300 as u
     from ufo_gb300 import workloads as W
     ring = W.c3_ring(u)

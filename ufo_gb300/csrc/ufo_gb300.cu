@@ -28,6 +28,14 @@
 
 namespace ufo {
 
+struct Parked {        // a particle in flight, moved between lanes or CTAs
+  double x, px, y, py, z, dp;
+  int64_t p;
+  int turn, target;
+  int seed;
+  int pad;
+};
+
 struct TrackArgs {
   const Op *ops;
   int n_ops;
@@ -47,7 +55,16 @@ struct TrackArgs {
   double *tracks;
   uint32_t *lost;
   double *final_state;
-  unsigned long long *queue;  // particles handed out so far
+  // queue[0]: particles handed out so far.  The compacting kernel also uses
+  // queue[1]: particles finished, queue[2]: CTAs that left, queue[3] / [4]:
+  // the particle pool's head and tail tickets (all zeroed by each launch)
+  unsigned long long *queue;
+  // particle pool of the compacting kernel (null: CTAs exchange nothing): a
+  // bounded ring of pool_cap slots; pool_seq[slot] = 2 e while the slot is free
+  // for ticket e * pool_cap + slot, 2 e + 1 once that ticket's particle is in it
+  Parked *pool;
+  unsigned long long *pool_seq;
+  long long pool_cap;
   // compacting kernel: chunks of 32 consecutive particles are handed out in
   // the order c -> (c * spread) mod (n / 32) (spread coprime to n / 32; 0: in
   // order; a last partial chunk comes last), so that a warp still takes
@@ -268,15 +285,60 @@ __global__ void __launch_bounds__(32) track_kernel(TrackArgs a) {
 // is set once and only read afterwards), so every barrier is reached by the
 // whole CTA.  Emptied warps stay in the loop (they take part in the barriers
 // and issue no FP64 work) until the CTA has no particle left.
-struct Parked {        // a particle in flight, moved between lanes
-  double x, px, y, py, z, dp;
-  int64_t p;
-  int turn, target;
-  int seed;
-  int pad;
-};
-
+// Phase B also balances the CTAs (when the launch gives a pool): the counter
+// runs out while each CTA holds whatever its lanes took, and an SM's turn
+// time grows with its busy warps, so the CTA holding the most survivors would
+// set the launch's time.  Every 4 turns each CTA compares its particles with
+// the share of the unfinished ones per CTA still running (rounded up to whole
+// warps): a CTA above it puts the excess into the pool, a CTA below it takes
+// from the pool.  The pool is a bounded ring with one sequence word per slot
+// (the multi-producer multi-consumer queue of D. Vyukov): warp 0 of a CTA
+// reserves free slots or claims filled ones with one CAS on the tail or head
+// ticket and gives up when the CAS or a slot's state says no, so no CTA ever
+// waits for another.  A CTA leaves when it holds no particle and the pool is
+// empty or its head slot is still being filled; the CTA filling it still
+// runs (it keeps at least one particle) and takes its own particles back
+// before it can leave, so no particle stays behind in the pool.
 constexpr int CTA_MAX_WARPS = 16;
+
+UFO_DEV void park(Parked &d, const State &s, int64_t p, int target, int sd) {
+  d.x = s.x; d.px = s.px; d.y = s.y; d.py = s.py; d.z = s.z; d.dp = s.dp;
+  d.p = p; d.turn = s.turn; d.target = target; d.seed = sd;
+}
+
+UFO_DEV void unpark(const Parked &d, const TrackArgs &a, State &s, int64_t &p, int &target,
+                    int &sd, const double *&tab) {
+  s.x = d.x; s.px = d.px; s.y = d.y; s.py = d.py; s.z = d.z; s.dp = d.dp;
+  s.o = dvd(1., add(s.dp, 1.));  // as load_particle: the same bits
+  s.opdp = add(1., s.dp);
+  s.bad_o = nf(s.o);
+  s.turn = d.turn;
+  p = d.p;
+  target = d.target;
+  sd = d.seed;
+  tab = a.table + static_cast<int64_t>(sd) * a.stride;
+}
+
+UFO_DEV unsigned long long vload(const unsigned long long *q) {
+  return *static_cast<const volatile unsigned long long *>(q);
+}
+
+// Warp 0: the number of consecutive slots from ticket t0 (at most `want`)
+// whose sequence word is `state` (0: free for that ticket, 1: filled with it).
+UFO_DEV int pool_run(const TrackArgs &a, unsigned long long t0, int want, unsigned state) {
+  const unsigned long long cap = static_cast<unsigned long long>(a.pool_cap);
+  const int lane = threadIdx.x & 31;
+  int n = 0;
+  while (n < want) {
+    const unsigned long long t = t0 + n + lane;
+    const bool ok = vload(a.pool_seq + t % cap) == 2 * (t / cap) + state;
+    const unsigned run = __ballot_sync(0xffffffffu, ok);
+    const int k = run == 0xffffffffu ? 32 : __ffs(~run) - 1;
+    n += k;
+    if (k < 32) break;
+  }
+  return n < want ? n : want;
+}
 
 template <bool FMA, bool FULL>
 __global__ void __launch_bounds__(CTA_MAX_WARPS * 32, 1) track_kernel_cta(TrackArgs a) {
@@ -285,9 +347,13 @@ __global__ void __launch_bounds__(CTA_MAX_WARPS * 32, 1) track_kernel_cta(TrackA
   // one phase ahead writes the other buffer)
   __shared__ int warp_active[2][CTA_MAX_WARPS];
   __shared__ int exhausted_flag;  // set once the work counter is exhausted
+  __shared__ unsigned long long seen[2];  // particles finished, CTAs that left
+  __shared__ unsigned long long xfer_base;  // first pool ticket moved
+  __shared__ int xfer_n, xfer_leave;        // particles moved; the CTA leaves
   const unsigned ALL = 0xffffffffu;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int nwarps = blockDim.x >> 5;
+  const int nthreads = static_cast<int>(blockDim.x);
   const unsigned lt_mask = (1u << lane) - 1u;
   volatile int *flag = &exhausted_flag;
   if (threadIdx.x == 0) *flag = 0;
@@ -327,14 +393,17 @@ __global__ void __launch_bounds__(CTA_MAX_WARPS * 32, 1) track_kernel_cta(TrackA
           if (sd < 0 || sd >= a.n_seeds) {  // seed outside the table: not tracked
             if (a.lost) a.lost[p] = 0xffffffffu;
             p = -1;
+            if (a.pool) atomicAdd(a.queue + 1, 1ull);  // finished (rare)
           } else if (target <= 0) {  // nothing to track
             store_final(s, a, p);
             p = -1;
+            if (a.pool) atomicAdd(a.queue + 1, 1ull);
           }
         }
       }
     }
     if (exhausted) break;  // warp-uniform
+    bool done = false;
     if (p >= 0) {  // a lane's particle needs no refill this turn
       one_turn<FMA, FULL>(s, a, tab, p);
       const bool lost = is_lost(s, a.mode);
@@ -342,11 +411,22 @@ __global__ void __launch_bounds__(CTA_MAX_WARPS * 32, 1) track_kernel_cta(TrackA
       if (lost || s.turn >= target) {
         store_final(s, a, p);
         p = -1;
+        done = true;
       }
+    }
+    if (a.pool) {  // launch-uniform: count the warp's finished particles
+      const unsigned f = __ballot_sync(ALL, done);
+      if (f && lane == 0) atomicAdd(a.queue + 1, static_cast<unsigned long long>(__popc(f)));
     }
   }
   // ---- phase B: one barrier per turn, survivors packed into the lowest warps
   for (int k = 0;; ++k) {
+    const bool exchange = a.pool != nullptr && gridDim.x > 1;  // launch-uniform
+    const bool balance = exchange && (k & 3) == 0;             // CTA-uniform
+    if (balance && threadIdx.x == 0) {  // read before the barrier: no extra one
+      seen[0] = vload(a.queue + 1);
+      seen[1] = vload(a.queue + 2);
+    }
     const unsigned act = __ballot_sync(ALL, p >= 0);
     if (lane == 0) warp_active[k & 1][warp] = __popc(act);
     __syncthreads();
@@ -357,29 +437,92 @@ __global__ void __launch_bounds__(CTA_MAX_WARPS * 32, 1) track_kernel_cta(TrackA
       total += c;
       busy += c > 0;
     }
-    if (total == 0) break;  // CTA-uniform: every thread read the same counts
-    if ((total + 31) / 32 < busy) {  // CTA-uniform: packing frees a warp
-      if (p >= 0) {
-        Parked &d = parked[before + __popc(act & lt_mask)];
-        d.x = s.x; d.px = s.px; d.y = s.y; d.py = s.py; d.z = s.z; d.dp = s.dp;
-        d.p = p; d.turn = s.turn; d.target = target; d.seed = sd;
+    if (total == 0 && !exchange) break;  // CTA-uniform: every thread read the same counts
+    // particles to move through the pool: > 0 take up to want, < 0 give -want
+    int want = 0;  // CTA-uniform
+    if (exchange) {
+      if (total == 0) {
+        want = nthreads;
+      } else if (balance) {
+        const long long running = static_cast<long long>(gridDim.x) - static_cast<long long>(seen[1]);
+        const long long unfinished = a.n - static_cast<long long>(seen[0]);
+        if (running > 0 && unfinished > 0) {
+          const long long share = (unfinished + running - 1) / running;
+          const long long whole = (share + 31) / 32 * 32;  // the warps the share needs
+          if (total > whole) {
+            want = -static_cast<int>(total - whole);
+          } else if (total < share) {
+            const long long room = (whole < nthreads ? whole : nthreads) - total;
+            want = room > 0 ? static_cast<int>(room) : 0;
+          }
+        }
+      }
+    }
+    if (want != 0) {  // CTA-uniform: every lane's particle goes through the slots
+      if (p >= 0) park(parked[before + __popc(act & lt_mask)], s, p, target, sd);
+      p = -1;  // the state lives in the slot now (nothing held across the pool step)
+      s = State{};
+      if (warp == 0) {
+        int n = 0, leave = 0;
+        unsigned long long t0 = 0;
+        if (want < 0) {  // reserve free slots at the tail
+          if (lane == 0) t0 = vload(a.queue + 4);
+          t0 = __shfl_sync(ALL, t0, 0);
+          n = pool_run(a, t0, -want, 0);
+          if (n > 0 && lane == 0 && atomicCAS(a.queue + 4, t0, t0 + n) != t0) n = -1;
+        } else {  // claim filled slots at the head
+          if (lane == 0) t0 = vload(a.queue + 3);
+          t0 = __shfl_sync(ALL, t0, 0);
+          n = pool_run(a, t0, want, 1);
+          leave = total == 0 && n == 0;  // empty, or its head is still being filled
+          if (n > 0 && lane == 0 && atomicCAS(a.queue + 3, t0, t0 + n) != t0) n = -1;
+        }
+        n = __shfl_sync(ALL, n, 0);  // -1: another CTA moved the ticket first
+        if (lane == 0) {
+          xfer_base = t0;
+          xfer_n = n > 0 ? n : 0;
+          xfer_leave = leave;
+          if (leave) atomicAdd(a.queue + 2, 1ull);
+        }
+        __threadfence();  // the claimed slots' contents before their readers
       }
       __syncthreads();
-      p = -1;
-      if (static_cast<int>(threadIdx.x) < total) {
-        const Parked &d = parked[threadIdx.x];
-        s.x = d.x; s.px = d.px; s.y = d.y; s.py = d.py; s.z = d.z; s.dp = d.dp;
-        s.o = dvd(1., add(s.dp, 1.));  // as load_particle: the same bits
-        s.opdp = add(1., s.dp);
-        s.bad_o = nf(s.o);
-        s.turn = d.turn;
-        p = d.p;
-        target = d.target;
-        sd = d.seed;
-        tab = a.table + static_cast<int64_t>(sd) * a.stride;
+      const int moved = xfer_n;
+      const unsigned long long t0 = xfer_base;
+      const unsigned long long cap = static_cast<unsigned long long>(a.pool_cap);
+      int keep = total;
+      if (want < 0) {  // the highest parked particles go to the reserved slots
+        keep = total - moved;
+        if (static_cast<int>(threadIdx.x) < moved) {
+          const unsigned long long t = t0 + threadIdx.x;
+          a.pool[t % cap] = parked[keep + threadIdx.x];
+          __threadfence();
+          *static_cast<volatile unsigned long long *>(a.pool_seq + t % cap) = 2 * (t / cap) + 1;
+        }
       }
+      if (static_cast<int>(threadIdx.x) < keep) {
+        unpark(parked[threadIdx.x], a, s, p, target, sd, tab);
+      } else if (want > 0 && static_cast<int>(threadIdx.x) < keep + moved) {
+        const unsigned long long t = t0 + (threadIdx.x - keep);
+        const unsigned long long *w = reinterpret_cast<const unsigned long long *>(a.pool + t % cap);
+        Parked d;
+        unsigned long long *dw = reinterpret_cast<unsigned long long *>(&d);
+#pragma unroll
+        for (int i = 0; i < static_cast<int>(sizeof(Parked) / 8); ++i) dw[i] = __ldcg(w + i);
+        unpark(d, a, s, p, target, sd, tab);
+        __threadfence();  // the slot is read before it is handed back
+        *static_cast<volatile unsigned long long *>(a.pool_seq + t % cap) = 2 * (t / cap + 1);
+      }
+      if (xfer_leave) break;  // CTA-uniform: no particle in the CTA
+      // the slots are rewritten only after the next phase's barrier
+    } else if ((total + 31) / 32 < busy) {  // CTA-uniform: packing frees a warp
+      if (p >= 0) park(parked[before + __popc(act & lt_mask)], s, p, target, sd);
+      __syncthreads();
+      p = -1;
+      if (static_cast<int>(threadIdx.x) < total) unpark(parked[threadIdx.x], a, s, p, target, sd, tab);
       // the slots are rewritten only after the next phase's barrier
     }
+    bool done = false;
     if (p >= 0) {
       one_turn<FMA, FULL>(s, a, tab, p);
       const bool lost = is_lost(s, a.mode);
@@ -387,7 +530,12 @@ __global__ void __launch_bounds__(CTA_MAX_WARPS * 32, 1) track_kernel_cta(TrackA
       if (lost || s.turn >= target) {
         store_final(s, a, p);
         p = -1;
+        done = true;
       }
+    }
+    if (exchange) {  // count the warp's finished particles
+      const unsigned f = __ballot_sync(ALL, done);
+      if (f && lane == 0) atomicAdd(a.queue + 1, static_cast<unsigned long long>(__popc(f)));
     }
   }
 }
@@ -575,6 +723,8 @@ struct ufo_ctx {
   int warps_per_sm;  // resident warps per SM of the persistent grid
   cudaStream_t stream;
   unsigned long long *queue;
+  ufo::Parked *pool;               // the compacting kernel's particle pool
+  unsigned long long *pool_seq;    // and its slots' sequence words
   std::atomic<int64_t> launches;
 };
 
@@ -838,7 +988,8 @@ int launch_kernels(ufo::TrackArgs &a, bool full, int sm_count, int warps_per_sm,
       full ? ufo::track_plain_kernel<false, true><<<blocks, 128, 0, stream>>>(a)
            : ufo::track_plain_kernel<false, false><<<blocks, 128, 0, stream>>>(a);
   } else if (a.flags & UFO_TRACK_COMPACT) {
-    UFO_CUDA(cudaMemsetAsync(a.queue, 0, sizeof(unsigned long long), stream));
+    // the work counter, the finished and departed counts, the pool's tickets
+    UFO_CUDA(cudaMemsetAsync(a.queue, 0, 5 * sizeof(unsigned long long), stream));
     // one CTA per SM (as many SMs as the particles' warps allow) of up to
     // warps_per_sm warps (at most 16); survivors are packed within each CTA
     const int64_t warps = (a.n + 31) / 32;
@@ -848,6 +999,12 @@ int launch_kernels(ufo::TrackArgs &a, bool full, int sm_count, int warps_per_sm,
     if (ctas * wpc > warps) wpc = static_cast<int>((warps + ctas - 1) / ctas);
     a.spread = spread_multiplier(a.n);
     const unsigned g = static_cast<unsigned>(ctas), tpb = static_cast<unsigned>(wpc * 32);
+    if (a.pool) {
+      // as many slots as the CTAs have lanes: the particles in flight once the
+      // counter is exhausted (the pool array holds sm_count * CTA_MAX_WARPS * 32)
+      a.pool_cap = static_cast<long long>(g) * tpb;
+      UFO_CUDA(cudaMemsetAsync(a.pool_seq, 0, sizeof(unsigned long long) * a.pool_cap, stream));
+    }
     const size_t smem = sizeof(ufo::Parked) * tpb;
     if (fma)
       full ? ufo::track_kernel_cta<true, true><<<g, tpb, smem, stream>>>(a)
@@ -899,6 +1056,9 @@ ufo::TrackArgs make_args(const ufo::Op *ops, int n_ops, const double *table, int
   a.lost = d_lost;
   a.final_state = d_final;
   a.queue = queue;
+  a.pool = nullptr;
+  a.pool_seq = nullptr;
+  a.pool_cap = 0;
   a.spread = 0;
   return a;
 }
@@ -911,6 +1071,8 @@ int launch_track(ufo_ctx *ctx, const ufo_prog *prog, const double *d_coords, con
   ufo::TrackArgs a = make_args(prog->ops, prog->n_ops, prog->table, prog->stride, prog->n_seeds,
                                prog->n_dumps, d_coords, d_seed, d_pturns, n, turns, mode, flags,
                                slots, every, d_tracks, d_lost, d_final, ctx->queue);
+  a.pool = ctx->pool;
+  a.pool_seq = ctx->pool_seq;
   const int rc = launch_kernels(a, prog->full, ctx->sm_count, ctx->warps_per_sm, stream);
   if (rc == UFO_OK) ctx->launches.fetch_add(1);
   return rc;
@@ -965,6 +1127,18 @@ int ufo_ctx_create(int device, ufo_ctx **out) {
     delete c;
     return fail(UFO_E_NOMEM, "cudaMalloc(queue): %s", cudaGetErrorString(e));
   }
+  // one pool slot per lane of the largest compacting grid
+  const size_t slots = static_cast<size_t>(c->sm_count) * ufo::CTA_MAX_WARPS * 32;
+  c->pool = nullptr;
+  c->pool_seq = nullptr;
+  if (cudaMalloc(&c->pool, sizeof(ufo::Parked) * slots) != cudaSuccess ||
+      cudaMalloc(&c->pool_seq, sizeof(unsigned long long) * slots) != cudaSuccess) {
+    cudaFree(c->pool);
+    cudaFree(c->queue);
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return fail(UFO_E_NOMEM, "cudaMalloc(particle pool of %zu slots)", slots);
+  }
   *out = c;
   return UFO_OK;
 }
@@ -974,6 +1148,8 @@ void ufo_ctx_destroy(ufo_ctx *ctx) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   cudaFree(ctx->queue);
+  cudaFree(ctx->pool);
+  cudaFree(ctx->pool_seq);
   cudaStreamDestroy(ctx->stream);
   delete ctx;
 }

@@ -240,26 +240,30 @@ class StableAperture:
         return C.reads_turn(self._c.prog)
 
     # resident warps per SM of the compacting kernel for a scan: measured
-    # best on the 196,608-particle dynamic-aperture grid (8 beat 12 and 16)
-    COMPACT_WARPS_PER_SM = 8
+    # best on the 196,608-particle dynamic-aperture grid with the CTAs
+    # exchanging particles (16: 8.1e9, 8: 7.8e9 particle*element*turns/s)
+    COMPACT_WARPS_PER_SM = 16
 
     def run(self, threads=1, compact=None):
-        """One launch of the CTA-compacting persistent kernel (default,
-        ``compact=None`` or ``True``): once every particle has been handed out,
-        each CTA packs its survivors into its lowest warps at every turn, so
-        the long-lived particles of an uneven scan fill whole warps.
-        ``compact='two-phase'``: track the first turns/8 with the full
+        """``compact='two-phase'`` (the default, ``compact=None``, for lattices
+        that do not read ``turn``): track the first turns/8 with the full
         persistent grid, then relaunch only the survivors on a grid sized to
-        them (not for lattices that read ``turn``).  ``compact=False``: one
-        launch of the one-warp persistent kernel.  Loss turns and coordinates
-        are the same in every case."""
+        them, whose warps run free of one another.  ``compact=True`` (the
+        default for lattices that read ``turn``, which a second phase would
+        renumber): one launch of the CTA-compacting persistent kernel; once
+        every particle has been handed out, each CTA packs its survivors into
+        its lowest warps at every turn and the CTAs even out their particle
+        counts through a pool, so the long-lived particles of an uneven scan
+        fill whole warps on every SM.  ``compact=False``: one launch of the
+        one-warp persistent kernel.  Loss turns and coordinates are the same
+        in every case."""
         pool = np.asarray(self.parameters, dtype=np.float64)
         seed_values, seed = self._c.seeds(pool)
         dprog = self._c.device(self.ctx, seed_values)
         coords = _coords_from_pool(pool, self._names, self.flags, self.dp)
         T, n = int(self.turns), coords.shape[0]
         if compact is None:
-            compact = True
+            compact = 'two-phase'
         if compact == 'two-phase' and self._uses_turn():
             compact = True
         flags = _track_flags(self.flags)
