@@ -40,8 +40,10 @@ extern "C" {
 #define UFO_TRACK_PLAIN 4    /* one thread per particle, no lane refill */
 #define UFO_TRACK_COMPACT 8  /* persistent CTAs (one per SM, warps_per_sm warps, at most
                                 16) that pack survivors into full warps once every particle
-                                is handed out; PLAIN takes precedence.  Every kernel gives
-                                the same results bit for bit. */
+                                is handed out and even out their particle counts through
+                                the context's particle pool (ufo_track_noalloc: packing
+                                within each CTA only); PLAIN takes precedence.  Every
+                                kernel gives the same results bit for bit. */
 
 #define UFO_OP_WORDS 8
 
@@ -55,7 +57,10 @@ const char *ufo_last_error(void);
 int ufo_device_count(int *count);
 
 /* Create a context on `device` with its own stream; replaces the OpenCL
- * context + command queue of ufo/cl_utils.py:30-33 and ufo/track.py:44-45. */
+ * context + command queue of ufo/cl_utils.py:30-33 and ufo/track.py:44-45.
+ * Holds the work counters and the compacting kernel's particle pool (80 bytes
+ * per lane of the largest compacting grid: SMs x 512, 6.2 MB on 152 SMs).
+ * Launches through one context share them: serialise them on one stream. */
 int ufo_ctx_create(int device, ufo_ctx **out);
 void ufo_ctx_destroy(ufo_ctx *ctx);
 
@@ -131,6 +136,8 @@ int ufo_track_device(ufo_ctx *ctx, const ufo_prog *prog, const double *d_coords,
  * by the lattice compiler (ufo_gb300/compiler.py).  A malformed program there
  * stays in bounds (the kernels bound their expression stacks) but gives a NaN
  * coefficient or a wrong loss test instead of an error.
+ * With UFO_TRACK_COMPACT the CTAs pack their survivors but exchange none: the
+ * particle pool they would exchange through belongs to a context.
  */
 int ufo_track_noalloc(const int32_t *ops, int n_ops, const double *d_table, int64_t stride,
                       int n_seeds, int n_dumps, const double *d_coords, const int32_t *d_seed,
