@@ -468,6 +468,43 @@ def test_compacting_kernel_is_bit_identical(fma):
     assert np.array_equal(out[0][1], pturns)  # nothing is lost in the C1 ring
 
 
+@pytest.mark.parametrize('fma', [False, True])
+def test_compacting_kernel_pool_exchange_is_bit_identical(fma):
+    """Uneven work per CTA once the work counter runs out: the particles of
+    every seventh chunk of 32 track 300 turns, the others 3.  The compacting
+    kernel's CTAs then hold from none to several chunks of long-lived
+    particles and even them out through the context's particle pool (CTAs
+    that run empty leave).  Loss turns and final coordinates equal the
+    one-warp and plain kernels' bit for bit, so every particle was finished
+    exactly once and none stayed behind in the pool."""
+    import ufo_gb300 as u
+    from ufo_gb300 import capi, compiler as C, workloads as W
+    ctx = u.context(0)
+    tf = capi.UFO_TRACK_FMA if fma else 0
+    ring = W.c1_ring(u)
+    dp = capi.DeviceProgram(ctx, C.compile_line(ring, u.KICK | (u.FMA if fma else 0),
+                                                where=[-1]))
+    n = 152 * 8 * 32 + 17
+    beam = W.c1_beam(n, seed=21)
+    pturns = np.where((np.arange(n) // 32) % 7 == 0, 300, 3).astype(np.int32)
+    before = ctx.warps_per_sm
+    out = {}
+    try:
+        for name, extra, warps in (('one-warp', 0, 16), ('plain', capi.UFO_TRACK_PLAIN, 16),
+                                   ('compact8', capi.UFO_TRACK_COMPACT, 8),
+                                   ('compact16', capi.UFO_TRACK_COMPACT, 16)):
+            ctx.set_tuning(warps)
+            out[name] = capi.track(ctx, dp, beam, 300, capi.UFO_MODE_TRACK, tf | extra,
+                                   pturns=pturns, slots=0)
+    finally:
+        ctx.set_tuning(before)
+    _, lost, final = out['one-warp']
+    assert np.array_equal(lost, pturns)  # nothing is lost in the C1 ring
+    for name in ('plain', 'compact8', 'compact16'):
+        assert np.array_equal(out[name][1], lost), name
+        assert np.array_equal(out[name][2], final, equal_nan=True), name
+
+
 def test_stable_aperture_with_turn_dependent_kicker_runs_in_one_phase():
     """A time-dependent element (the HOWTO's gate kicker, firing on turn 20)
     reads ``turn``: StableAperture must not restart turn numbers in a second
