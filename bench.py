@@ -691,9 +691,10 @@ def bench_c3(args):
                                          all(np.array_equal(a[1], lost_p)
                                              for a in api.values())),
             'gpu_launches': launches,
+            # the second phase copies the survivors in and out once more
             'e2e': {'value': pet / api['two-phase'][0], 'unit': 'particle*element*turns/s',
-                    'h2d_bytes_per_step': n * 6 * 8,
-                    'd2h_bytes_per_step': n * (6 * 8 + 4),
+                    'h2d_bytes_per_step': (n + (api['two-phase'][3] or 0)) * 6 * 8,
+                    'd2h_bytes_per_step': (n + (api['two-phase'][3] or 0)) * (6 * 8 + 4),
                     'api': 'ufo_gb300.StableAperture(...).run() (two-phase compaction, the '
                            'default; host buffers)'}}
     if clk:
@@ -769,6 +770,8 @@ def c3_measure(ctx, stream, mode, reps=2):
     t0 = time.perf_counter()
     sa.run()
     e2e_s = time.perf_counter() - t0
+    # the two-phase run copies the survivors of its first phase in and out once more
+    n_io = n + (getattr(sa, 'survivors_after_first_phase', None) or 0)
     identical &= bool(np.array_equal(sa.lost.astype(np.int64), lost_strict))
     peak = ctypes_peak(ctx)
     prog = C.compile_line(ring, u.KICK | (u.FMA if mode == 'fma' else 0), where=[-1])
@@ -796,7 +799,7 @@ def c3_measure(ctx, stream, mode, reps=2):
         'loss_turns_note': 'every variant and the public API give, for all 196,608 particles, '
                            'the loss turns of the strict (bit-identical) arithmetic',
         'e2e': {'value': pet / e2e_s, 'unit': 'particle*element*turns/s', 's': e2e_s,
-                'h2d_bytes_per_step': n * 6 * 8, 'd2h_bytes_per_step': n * (6 * 8 + 4),
+                'h2d_bytes_per_step': n_io * 6 * 8, 'd2h_bytes_per_step': n_io * (6 * 8 + 4),
                 'api': 'ufo_gb300.StableAperture(...).run() (two-phase compaction, the default; '
                        'host buffers)'}}
 
